@@ -1,0 +1,144 @@
+"""ctypes bindings of include/igxrt.h (the engine's C ABI).
+
+The library is loaded from this package directory.  There is no fallback:
+if libigxrt.so is missing, importing the package raises, because every query
+must run on the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libigxrt.so")
+
+NO_HIT = np.float32(3.4028235e38)
+NO_RAY_HIT = 0xFFFFFFFF
+
+LAYOUT_BVH2 = 0
+LAYOUT_BVH4 = 1
+LAYOUT_COUNT = 2
+TRACE_HOST_MEMORY = 1
+
+STATUS = {
+    0: "IGXRT_OK",
+    1: "IGXRT_ERROR_INVALID_ARGUMENT",
+    2: "IGXRT_ERROR_CUDA",
+    3: "IGXRT_ERROR_OUT_OF_MEMORY",
+    4: "IGXRT_ERROR_INVALID_BVH",
+    5: "IGXRT_ERROR_KERNEL_STATUS",
+    6: "IGXRT_ERROR_ADMISSION",
+    7: "IGXRT_ERROR_TIMEOUT",
+    8: "IGXRT_ERROR_UNSUPPORTED",
+    9: "IGXRT_ERROR_NOT_READY",
+    10: "IGXRT_ERROR_IO",
+}
+
+# numpy views of the ABI records (little-endian, packed exactly as the C structs)
+TRIANGLE_DTYPE = np.dtype([("p0", "<f4", (3,)), ("n0", "<u4"), ("p1", "<f4", (3,)), ("n1", "<u4"),
+                           ("p2", "<f4", (3,)), ("n2", "<u4")])
+RAY_DTYPE = np.dtype([("org", "<f4", (3,)), ("tmin", "<f4"), ("dir", "<f4", (3,)), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])
+PRIM_RECORD_DTYPE = np.dtype([("p0", "<f4", (3,)), ("prim", "<u4"), ("e1", "<f4", (3,)),
+                              ("leaf_end", "<u4"), ("e2", "<f4", (3,)), ("pad", "<u4")])
+BVH2_NODE_DTYPE = np.dtype([("c0_x", "<f4", (2,)), ("c0_y", "<f4", (2,)), ("c1_x", "<f4", (2,)),
+                            ("c1_y", "<f4", (2,)), ("c0_z", "<f4", (2,)), ("c1_z", "<f4", (2,)),
+                            ("child", "<i4", (2,)), ("pad", "<u4", (2,))])
+BVH4_NODE_DTYPE = np.dtype([("lo_x", "<f4", (4,)), ("hi_x", "<f4", (4,)), ("lo_y", "<f4", (4,)),
+                            ("hi_y", "<f4", (4,)), ("lo_z", "<f4", (4,)), ("hi_z", "<f4", (4,)),
+                            ("child", "<i4", (4,)), ("pad", "<u4", (4,))])
+assert TRIANGLE_DTYPE.itemsize == 48 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.itemsize == 16
+assert PRIM_RECORD_DTYPE.itemsize == 48 and BVH2_NODE_DTYPE.itemsize == 64
+assert BVH4_NODE_DTYPE.itemsize == 128
+
+
+class BuildOptions(C.Structure):
+    _fields_ = [("max_leaf_size", C.c_uint32), ("sah_bins", C.c_uint32), ("node_cost", C.c_float),
+                ("tri_cost", C.c_float), ("threads", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+class BvhInfo(C.Structure):
+    _fields_ = [("triangle_count", C.c_uint32), ("bvh2_nodes", C.c_uint32),
+                ("bvh4_nodes", C.c_uint32), ("leaf_count", C.c_uint32), ("max_depth", C.c_uint32),
+                ("max_leaf_size", C.c_uint32), ("sah_cost", C.c_float), ("bounds", C.c_float * 6),
+                ("pad_abs", C.c_float), ("max_stack", C.c_uint32 * LAYOUT_COUNT),
+                ("device_bytes", C.c_uint64)]
+
+
+class LaunchParams(C.Structure):
+    _fields_ = [("block_size", C.c_uint32), ("stack_depth", C.c_uint32),
+                ("packet_size", C.c_uint32), ("layout", C.c_uint32), ("ctas_per_sm", C.c_uint32),
+                ("reserved", C.c_uint32 * 3)]
+
+
+_vp = C.c_void_p
+_u32 = C.c_uint32
+_u64 = C.c_uint64
+_i32 = C.c_int
+_st = C.c_int
+
+# (name, restype, argtypes) for every entry point of include/igxrt.h.
+PROTOTYPES = [
+    ("igxrt_bvh_build", _st, [_vp, _u32, C.POINTER(BuildOptions), C.POINTER(_vp)]),
+    ("igxrt_bvh_destroy", _st, [_vp]),
+    ("igxrt_bvh_get_info", _st, [_vp, C.POINTER(BvhInfo)]),
+    ("igxrt_bvh_get_data", _st, [_vp, _u32, C.POINTER(_vp), C.POINTER(_u64), C.POINTER(_vp),
+                                 C.POINTER(_u64)]),
+    ("igxrt_bvh_validate", _st, [_vp, C.c_char_p, C.c_size_t]),
+    ("igxrt_bvh_save", _st, [_vp, C.c_char_p]),
+    ("igxrt_bvh_load", _st, [C.c_char_p, C.POINTER(_vp)]),
+    ("igxrt_create", _st, [_i32, C.POINTER(_vp)]),
+    ("igxrt_destroy", _st, [_vp]),
+    ("igxrt_last_error", C.c_char_p, [_vp]),
+    ("igxrt_status_string", C.c_char_p, [_st]),
+    ("igxrt_scene_create", _st, [_vp, _vp, _u32, C.POINTER(BuildOptions), C.POINTER(_vp)]),
+    ("igxrt_scene_create_from_bvh", _st, [_vp, _vp, C.POINTER(_vp)]),
+    ("igxrt_scene_destroy", _st, [_vp]),
+    ("igxrt_scene_get_info", _st, [_vp, C.POINTER(BvhInfo)]),
+    ("igxrt_set_launch_params", _st, [_vp, C.POINTER(LaunchParams)]),
+    ("igxrt_get_launch_params", _st, [_vp, C.POINTER(LaunchParams)]),
+    ("igxrt_trace_closest", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _u32, _vp]),
+    ("igxrt_trace_any", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _u32, _vp]),
+    ("igxrt_fetch_hits", _st, [_vp, _vp, _u32, _vp, _vp]),
+    ("igxrt_sync", _st, [_vp, _vp]),
+    ("igxrt_count_fetches", _st, [_vp, _vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp]),
+]
+
+
+class IgxrtError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libigxrt.so (raising if it was never built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build the CUDA engine first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        h = C.CDLL(LIB_PATH)
+        for name, res, args in PROTOTYPES:
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def check(status: int, ctx=None, what: str = "") -> None:
+    if status != 0:
+        msg = ""
+        if ctx:
+            raw = lib().igxrt_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        if not msg:
+            msg = lib().igxrt_status_string(status).decode()
+        raise IgxrtError(status, f"{what}: {msg}" if what else msg)

@@ -1,0 +1,321 @@
+"""Host-side API of the ray-query engine, mirroring igx_raytracing's traversal.
+
+The reference exposes its ray queries as two GLSL functions,
+traceGeometry(ray, prevHit) -> Hit and traceOcclusion(ray, maxDist, prevHit)
+-> bool (res/shaders/trace.glsl:9-66, 70-98), evaluated per thread by the
+raygen and shadow dispatches.  Here the same queries take a whole batch:
+
+    ctx = Context()
+    scene = ctx.create_scene(triangles)          # SceneGraph buffers + BVH
+    hits = scene.trace_geometry(rays, prev_hit)  # traceGeometry per ray
+    occ = scene.trace_occlusion(rays, prev_hit)  # traceOcclusion, maxDist = ray.tmax
+
+Arrays may be numpy (host memory: staged by the library) or CUDA torch
+tensors (device memory: stream-ordered on torch's current stream).  Every
+call runs the CUDA kernels of libigxrt.so; there is no host fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _capi
+from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, RAY_DTYPE, TRACE_HOST_MEMORY,
+                    TRIANGLE_DTYPE, BuildOptions, BvhInfo, IgxrtError, LaunchParams, check, lib)
+
+try:  # torch is only needed for device-memory calls
+    import torch
+except Exception:  # pragma: no cover - torch is present in every supported image
+    torch = None
+
+
+def _is_cuda_tensor(x) -> bool:
+    return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
+
+
+def as_triangles(tris) -> np.ndarray:
+    """Accepts a TRIANGLE_DTYPE array, or (N,3,3) / (N,9) vertex positions."""
+    a = np.asarray(tris)
+    if a.dtype == TRIANGLE_DTYPE:
+        return np.ascontiguousarray(a)
+    a = np.asarray(a, dtype=np.float32)
+    if a.ndim == 2 and a.shape[1] == 9:
+        a = a.reshape(-1, 3, 3)
+    if a.ndim != 3 or a.shape[1:] != (3, 3):
+        raise ValueError("triangles must be TRIANGLE_DTYPE records or (N, 3, 3) vertices")
+    out = np.zeros(a.shape[0], dtype=TRIANGLE_DTYPE)
+    out["p0"], out["p1"], out["p2"] = a[:, 0], a[:, 1], a[:, 2]
+    return out
+
+
+def as_rays(rays) -> np.ndarray:
+    """Accepts a RAY_DTYPE array or an (N, 8) float32 array {org, tmin, dir, tmax}."""
+    a = np.asarray(rays)
+    if a.dtype == RAY_DTYPE:
+        return np.ascontiguousarray(a)
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] != 8:
+        raise ValueError("rays must be RAY_DTYPE records or an (N, 8) float32 array")
+    return a.view(RAY_DTYPE).reshape(-1)
+
+
+def make_rays(org, dirs, tmin=0.0, tmax=float(_capi.NO_HIT)) -> np.ndarray:
+    org = np.asarray(org, dtype=np.float32).reshape(-1, 3)
+    dirs = np.asarray(dirs, dtype=np.float32).reshape(-1, 3)
+    r = np.zeros(len(org), dtype=RAY_DTYPE)
+    r["org"], r["dir"] = org, dirs
+    r["tmin"], r["tmax"] = tmin, tmax
+    return r
+
+
+def _build_options(max_leaf_size=0, sah_bins=0, node_cost=0.0, tri_cost=0.0, threads=0):
+    o = BuildOptions()
+    o.max_leaf_size, o.sah_bins = max_leaf_size, sah_bins
+    o.node_cost, o.tri_cost, o.threads = node_cost, tri_cost, threads
+    return o
+
+
+def _info_dict(info: BvhInfo) -> dict:
+    return {
+        "triangle_count": info.triangle_count, "bvh2_nodes": info.bvh2_nodes,
+        "bvh4_nodes": info.bvh4_nodes, "leaf_count": info.leaf_count,
+        "max_depth": info.max_depth, "max_leaf_size": info.max_leaf_size,
+        "sah_cost": info.sah_cost, "bounds": list(info.bounds), "pad_abs": info.pad_abs,
+        "max_stack": list(info.max_stack), "device_bytes": info.device_bytes,
+    }
+
+
+class BVH:
+    """A BVH built on the host (no GPU needed): igxrt_bvh_*."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def build(cls, triangles, **opts) -> "BVH":
+        tris = as_triangles(triangles)
+        h = C.c_void_p()
+        o = _build_options(**opts)
+        check(lib().igxrt_bvh_build(tris.ctypes.data if len(tris) else None, len(tris),
+                                    C.byref(o), C.byref(h)), what="igxrt_bvh_build")
+        return cls(h.value)
+
+    @classmethod
+    def load(cls, path: str) -> "BVH":
+        h = C.c_void_p()
+        check(lib().igxrt_bvh_load(path.encode(), C.byref(h)), what=f"igxrt_bvh_load({path})")
+        return cls(h.value)
+
+    def save(self, path: str) -> None:
+        check(lib().igxrt_bvh_save(self._h, path.encode()), what=f"igxrt_bvh_save({path})")
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().igxrt_bvh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def info(self) -> dict:
+        i = BvhInfo()
+        check(lib().igxrt_bvh_get_info(self._h, C.byref(i)))
+        return _info_dict(i)
+
+    def arrays(self, layout: int = LAYOUT_BVH2):
+        """Copies of (nodes, prim records) in the export format of include/igxrt.h."""
+        nodes, nn, prims, np_ = C.c_void_p(), C.c_uint64(), C.c_void_p(), C.c_uint64()
+        check(lib().igxrt_bvh_get_data(self._h, layout, C.byref(nodes), C.byref(nn),
+                                       C.byref(prims), C.byref(np_)))
+        ndt = _capi.BVH2_NODE_DTYPE if layout == LAYOUT_BVH2 else _capi.BVH4_NODE_DTYPE
+        node_arr = np.zeros(nn.value, dtype=ndt)
+        prim_arr = np.zeros(np_.value, dtype=_capi.PRIM_RECORD_DTYPE)
+        if nn.value:
+            C.memmove(node_arr.ctypes.data, nodes.value, nn.value * ndt.itemsize)
+        if np_.value:
+            C.memmove(prim_arr.ctypes.data, prims.value, np_.value * 48)
+        return node_arr, prim_arr
+
+    def validate(self) -> None:
+        buf = C.create_string_buffer(512)
+        st = lib().igxrt_bvh_validate(self._h, buf, 512)
+        if st != 0:
+            raise IgxrtError(st, buf.value.decode())
+
+
+class Scene:
+    """A BVH resident in device memory, traced through its context."""
+
+    def __init__(self, ctx: "Context", handle: int, ntris: int):
+        self.ctx = ctx
+        self._h = C.c_void_p(handle)
+        self.triangle_count = ntris
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def info(self) -> dict:
+        i = BvhInfo()
+        check(lib().igxrt_scene_get_info(self._h, C.byref(i)))
+        return _info_dict(i)
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().igxrt_scene_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # Mirrors of the reference's GLSL entry points -------------------------
+    def trace_geometry(self, rays, prev_hit=None, stream=None):
+        """traceGeometry (trace.glsl:9-66) for every ray: closest hits."""
+        return self.ctx.trace_closest(self, rays, prev_hit, stream=stream)
+
+    def trace_occlusion(self, rays, prev_hit=None, stream=None):
+        """traceOcclusion (trace.glsl:70-98) for every ray, maxDist = ray.tmax."""
+        return self.ctx.trace_any(self, rays, prev_hit, stream=stream)
+
+
+class Context:
+    """igxrt_create / igxrt_destroy: one device, launch parameters, staging."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().igxrt_create(device, C.byref(h)), what=f"igxrt_create(device={device})")
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().igxrt_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- launch parameters -------------------------------------------------
+    @property
+    def launch_params(self) -> dict:
+        p = LaunchParams()
+        check(lib().igxrt_get_launch_params(self._h, C.byref(p)), self._h)
+        return {"block_size": p.block_size, "stack_depth": p.stack_depth,
+                "packet_size": p.packet_size, "layout": p.layout, "ctas_per_sm": p.ctas_per_sm}
+
+    def set_launch_params(self, **kw) -> None:
+        cur = self.launch_params
+        cur.update(kw)
+        p = LaunchParams()
+        for k, v in cur.items():
+            setattr(p, k, int(v))
+        check(lib().igxrt_set_launch_params(self._h, C.byref(p)), self._h, "set_launch_params")
+
+    # -- scenes ------------------------------------------------------------
+    def create_scene(self, triangles=None, bvh: Optional[BVH] = None, **opts) -> Scene:
+        h = C.c_void_p()
+        if bvh is not None:
+            check(lib().igxrt_scene_create_from_bvh(self._h, bvh.handle, C.byref(h)), self._h,
+                  "igxrt_scene_create_from_bvh")
+            return Scene(self, h.value, bvh.info["triangle_count"])
+        tris = as_triangles(triangles)
+        o = _build_options(**opts)
+        check(lib().igxrt_scene_create(self._h, tris.ctypes.data if len(tris) else None,
+                                       len(tris), C.byref(o), C.byref(h)), self._h,
+              "igxrt_scene_create")
+        return Scene(self, h.value, len(tris))
+
+    # -- queries -----------------------------------------------------------
+    @staticmethod
+    def _stream(stream, device_call: bool):
+        if stream is not None:
+            return C.c_void_p(int(stream))
+        if device_call and torch is not None:
+            return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        return C.c_void_p(0)
+
+    def _trace(self, scene: Scene, rays, prev_hit, mode: int, stream, out=None):
+        fn = lib().igxrt_trace_closest if mode == 0 else lib().igxrt_trace_any
+        if _is_cuda_tensor(rays):
+            assert rays.dtype == torch.float32 and rays.is_contiguous() and rays.shape[-1] == 8
+            n = rays.shape[0]
+            if out is None:
+                out = (torch.empty((n, 4), dtype=torch.float32, device=rays.device) if mode == 0
+                       else torch.empty(n, dtype=torch.int32, device=rays.device))
+            prev_ptr = None
+            if prev_hit is not None:
+                assert _is_cuda_tensor(prev_hit) and prev_hit.dtype == torch.int32
+                prev_ptr = prev_hit.data_ptr()
+            st = fn(self._h, scene.handle, rays.data_ptr(), prev_ptr, n, out.data_ptr(), 0,
+                    self._stream(stream, True))
+            check(st, self._h, "trace")
+            return out
+        r = as_rays(rays)
+        n = len(r)
+        prev = None
+        if prev_hit is not None:
+            prev = np.ascontiguousarray(prev_hit, dtype=np.uint32)
+            if len(prev) != n:
+                raise ValueError("prev_hit must have one entry per ray")
+        if out is None:
+            out = np.empty(n, dtype=HIT_DTYPE) if mode == 0 else np.empty(n, dtype=np.uint32)
+        if n == 0:
+            return out
+        st = fn(self._h, scene.handle, r.ctypes.data, prev.ctypes.data if prev is not None else None,
+                n, out.ctypes.data, TRACE_HOST_MEMORY, self._stream(stream, False))
+        check(st, self._h, "trace")
+        return out
+
+    def trace_closest(self, scene: Scene, rays, prev_hit=None, stream=None, out=None):
+        return self._trace(scene, rays, prev_hit, 0, stream, out)
+
+    def trace_any(self, scene: Scene, rays, prev_hit=None, stream=None, out=None):
+        return self._trace(scene, rays, prev_hit, 1, stream, out)
+
+    def count_fetches(self, scene: Scene, rays, prev_hit=None, mode: int = 0,
+                      layout: int = LAYOUT_BVH2):
+        """Node and primitive records the kernel fetches per ray (host arrays)."""
+        r = as_rays(rays)
+        n = len(r)
+        nf = np.zeros(n, dtype=np.uint32)
+        pf = np.zeros(n, dtype=np.uint32)
+        prev = None if prev_hit is None else np.ascontiguousarray(prev_hit, dtype=np.uint32)
+        if n:
+            check(lib().igxrt_count_fetches(
+                self._h, scene.handle, r.ctypes.data, prev.ctypes.data if prev is not None else None,
+                n, mode, layout, nf.ctypes.data, pf.ctypes.data, None), self._h, "count_fetches")
+        return nf, pf
+
+    def sync(self, stream=None) -> None:
+        check(lib().igxrt_sync(self._h, self._stream(stream, True)), self._h, "sync")
+
+
+__all__ = ["BVH", "Context", "Scene", "IgxrtError", "as_rays", "as_triangles", "make_rays",
+           "LAYOUT_BVH2", "LAYOUT_BVH4"]

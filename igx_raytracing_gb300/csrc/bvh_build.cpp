@@ -1,0 +1,866 @@
+// bvh_build.cpp — host BVH builder, validator and (de)serialiser.
+//
+// The reference has no acceleration structure: traceGeometry and
+// traceOcclusion (res/shaders/trace.glsl:9-98) test every primitive.  This
+// builder produces the BVH the CUDA kernels traverse instead:
+//   * binned SAH over triangle centroids (32 bins by default), leaves of at
+//     most `max_leaf_size` triangles, a median split below depth
+//     kMaxDepth - 24 so the depth stays bounded;
+//   * the BVH2 layout (64-byte nodes with both child boxes) and a BVH4 layout
+//     (128-byte nodes) collapsed from the same binary tree, sharing one array
+//     of 48-byte primitive records in leaf order;
+//   * every box widened outward by pad_abs = 2^-18 * max|coordinate| so the
+//     kernels' binary32 slab test never culls a box whose triangle the
+//     reference's test would accept (rounding of the slab distances is below
+//     2^-23 * max|coordinate| for ray origins within that magnitude).
+// Host code is compiled with -ffp-contract=off so the tree is bit-identical on
+// every host architecture.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <thread>
+
+#include "internal.h"
+
+namespace igxrt {
+
+std::string format(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    return std::string(buf);
+}
+
+namespace {
+
+constexpr float kInf = INFINITY;
+
+struct Aabb {
+    float lo[3], hi[3];
+    void reset() {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = kInf;
+            hi[a] = -kInf;
+        }
+    }
+    void grow(const Aabb& b) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], b.lo[a]);
+            hi[a] = std::max(hi[a], b.hi[a]);
+        }
+    }
+    void grow_point(const float* p) {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], p[a]);
+            hi[a] = std::max(hi[a], p[a]);
+        }
+    }
+    // Half surface area; 0 for an empty box.
+    float half_area() const {
+        if (!(hi[0] >= lo[0]))
+            return 0.f;
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+struct BNode {
+    Aabb box;
+    uint32_t left = 0, right = 0;
+    uint32_t first = 0, count = 0;  // count > 0: leaf over refs[first, first+count)
+    bool leaf() const { return count > 0; }
+};
+
+struct Builder {
+    const igxrt_triangle* tris = nullptr;
+    uint32_t n = 0;
+    uint32_t max_leaf = 8;
+    uint32_t bins = 32;
+    float cn = 1.f, ct = 1.f;
+    std::vector<Aabb> tb;
+    std::vector<float> cen;  // 3 per triangle
+    std::vector<uint32_t> refs;
+    std::vector<BNode> nodes;
+    std::atomic<uint32_t> node_count{0};
+    std::atomic<int> spare_threads{0};
+
+    uint32_t build(uint32_t begin, uint32_t end, uint32_t depth);
+    uint32_t split_median(uint32_t begin, uint32_t end, const Aabb& cb);
+};
+
+uint32_t Builder::split_median(uint32_t begin, uint32_t end, const Aabb& cb) {
+    int axis = 0;
+    float best = -1.f;
+    for (int a = 0; a < 3; ++a) {
+        const float e = cb.hi[a] - cb.lo[a];
+        if (e > best) {
+            best = e;
+            axis = a;
+        }
+    }
+    const uint32_t mid = begin + (end - begin) / 2;
+    const float* c = cen.data();
+    std::nth_element(refs.begin() + begin, refs.begin() + mid, refs.begin() + end,
+                     [c, axis](uint32_t x, uint32_t y) {
+                         const float cx = c[3 * x + axis], cy = c[3 * y + axis];
+                         return cx < cy || (cx == cy && x < y);
+                     });
+    return mid;
+}
+
+uint32_t Builder::build(uint32_t begin, uint32_t end, uint32_t depth) {
+    const uint32_t id = node_count.fetch_add(1);
+    BNode& nd = nodes[id];
+    const uint32_t cnt = end - begin;
+    Aabb box, cb;
+    box.reset();
+    cb.reset();
+    for (uint32_t i = begin; i < end; ++i) {
+        const uint32_t r = refs[i];
+        box.grow(tb[r]);
+        cb.grow_point(&cen[3 * r]);
+    }
+    nd.box = box;
+    auto make_leaf = [&]() {
+        nd.first = begin;
+        nd.count = cnt;
+        return id;
+    };
+    if (cnt == 1)
+        return make_leaf();
+
+    uint32_t mid = begin;
+    if (depth + 24 >= kMaxDepth) {
+        if (cnt <= max_leaf)
+            return make_leaf();
+        mid = split_median(begin, end, cb);
+    } else {
+        float best_cost = kInf;
+        int best_axis = -1;
+        uint32_t best_bin = 0;
+        std::vector<uint32_t> bcount(bins);
+        std::vector<Aabb> bbox(bins);
+        std::vector<float> right_area(bins);
+        std::vector<uint32_t> right_count(bins);
+        for (int a = 0; a < 3; ++a) {
+            const float ext = cb.hi[a] - cb.lo[a];
+            if (!(ext > 0.f))
+                continue;
+            const float scale = (float)bins / ext;
+            const float cmin = cb.lo[a];
+            std::fill(bcount.begin(), bcount.end(), 0u);
+            for (auto& b : bbox)
+                b.reset();
+            for (uint32_t i = begin; i < end; ++i) {
+                const uint32_t r = refs[i];
+                int b = (int)((cen[3 * r + a] - cmin) * scale);
+                b = std::min(std::max(b, 0), (int)bins - 1);
+                ++bcount[b];
+                bbox[b].grow(tb[r]);
+            }
+            Aabb acc;
+            acc.reset();
+            uint32_t nacc = 0;
+            for (int b = (int)bins - 1; b > 0; --b) {
+                acc.grow(bbox[b]);
+                nacc += bcount[b];
+                right_area[b] = acc.half_area();
+                right_count[b] = nacc;
+            }
+            acc.reset();
+            nacc = 0;
+            for (uint32_t b = 0; b + 1 < bins; ++b) {
+                acc.grow(bbox[b]);
+                nacc += bcount[b];
+                const uint32_t nr = right_count[b + 1];
+                if (nacc == 0 || nr == 0)
+                    continue;
+                const float cost = acc.half_area() * (float)nacc + right_area[b + 1] * (float)nr;
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best_axis = a;
+                    best_bin = b;
+                }
+            }
+        }
+        if (best_axis < 0) {
+            // All centroids coincide: no SAH plane separates them.
+            if (cnt <= max_leaf)
+                return make_leaf();
+            mid = begin + cnt / 2;
+        } else {
+            const float parent_area = box.half_area();
+            const float split_cost =
+                parent_area > 0.f ? cn + ct * best_cost / parent_area : cn + ct * (float)cnt;
+            const float leaf_cost = ct * (float)cnt;
+            if (cnt <= max_leaf && leaf_cost <= split_cost)
+                return make_leaf();
+            const float scale = (float)bins / (cb.hi[best_axis] - cb.lo[best_axis]);
+            const float cmin = cb.lo[best_axis];
+            const float* c = cen.data();
+            const int ax = best_axis;
+            const uint32_t bb = best_bin, nb = bins;
+            auto it = std::partition(refs.begin() + begin, refs.begin() + end, [&](uint32_t r) {
+                int b = (int)((c[3 * r + ax] - cmin) * scale);
+                b = std::min(std::max(b, 0), (int)nb - 1);
+                return (uint32_t)b <= bb;
+            });
+            mid = (uint32_t)(it - refs.begin());
+            if (mid == begin || mid == end)
+                mid = split_median(begin, end, cb);
+        }
+    }
+
+    uint32_t l = 0, r = 0;
+    bool spawned = false;
+    std::thread worker;
+    if (cnt >= 65536) {
+        int s = spare_threads.load();
+        while (s > 0 && !spare_threads.compare_exchange_weak(s, s - 1)) {
+        }
+        if (s > 0) {
+            spawned = true;
+            worker = std::thread([&]() {
+                l = build(begin, mid, depth + 1);
+                spare_threads.fetch_add(1);
+            });
+        }
+    }
+    if (!spawned)
+        l = build(begin, mid, depth + 1);
+    r = build(mid, end, depth + 1);
+    if (spawned)
+        worker.join();
+    nd.left = l;
+    nd.right = r;
+    return id;
+}
+
+struct Layout {
+    const Builder& b;
+    igxrt_bvh& out;
+    float pad;
+    std::vector<uint32_t> leaf_rec;  // build node -> first primitive record
+    uint32_t max_depth = 0;
+    double sah_nodes = 0, sah_tris = 0;
+
+    void set_box(float* lo_hi_x, float* lo_hi_y, float* lo_hi_z, const Aabb& a) const {
+        lo_hi_x[0] = a.lo[0] - pad;
+        lo_hi_x[1] = a.hi[0] + pad;
+        lo_hi_y[0] = a.lo[1] - pad;
+        lo_hi_y[1] = a.hi[1] + pad;
+        lo_hi_z[0] = a.lo[2] - pad;
+        lo_hi_z[1] = a.hi[2] + pad;
+    }
+
+    int32_t emit_leaf(uint32_t id) {
+        const BNode& nd = b.nodes[id];
+        const uint32_t first = (uint32_t)out.prims.size();
+        leaf_rec[id] = first;
+        for (uint32_t k = 0; k < nd.count; ++k) {
+            const uint32_t t = b.refs[nd.first + k];
+            const igxrt_triangle& tri = b.tris[t];
+            igxrt_prim_record rec;
+            for (int a = 0; a < 3; ++a) {
+                rec.p0[a] = tri.p0[a];
+                rec.e1[a] = tri.p1[a] - tri.p0[a];
+                rec.e2[a] = tri.p2[a] - tri.p0[a];
+            }
+            rec.prim = t;
+            rec.leaf_end = (k + 1 == nd.count) ? 1u : 0u;
+            rec.pad = 0;
+            out.prims.push_back(rec);
+        }
+        return ~(int32_t)first;
+    }
+
+    int32_t emit2(uint32_t id, uint32_t depth) {
+        const BNode& nd = b.nodes[id];
+        max_depth = std::max(max_depth, depth);
+        const uint32_t idx = (uint32_t)out.nodes2.size();
+        out.nodes2.push_back(igxrt_bvh2_node{});
+        const uint32_t kids[2] = {nd.left, nd.right};
+        int32_t refs[2];
+        for (int c = 0; c < 2; ++c) {
+            const BNode& k = b.nodes[kids[c]];
+            refs[c] = k.leaf() ? emit_leaf(kids[c]) : emit2(kids[c], depth + 1);
+        }
+        igxrt_bvh2_node& o = out.nodes2[idx];
+        set_box(o.c0_x, o.c0_y, o.c0_z, b.nodes[kids[0]].box);
+        set_box(o.c1_x, o.c1_y, o.c1_z, b.nodes[kids[1]].box);
+        o.child[0] = refs[0];
+        o.child[1] = refs[1];
+        o.pad[0] = o.pad[1] = 0;
+        return (int32_t)idx;
+    }
+
+    int32_t emit4(uint32_t id) {
+        std::vector<uint32_t> kids = {b.nodes[id].left, b.nodes[id].right};
+        while (kids.size() < 4) {
+            int pick = -1;
+            float best = -1.f;
+            for (size_t k = 0; k < kids.size(); ++k) {
+                const BNode& c = b.nodes[kids[k]];
+                if (!c.leaf() && c.box.half_area() > best) {
+                    best = c.box.half_area();
+                    pick = (int)k;
+                }
+            }
+            if (pick < 0)
+                break;
+            const BNode& c = b.nodes[kids[pick]];
+            const uint32_t l = c.left, r = c.right;
+            kids[pick] = l;
+            kids.insert(kids.begin() + pick + 1, r);
+        }
+        const uint32_t idx = (uint32_t)out.nodes4.size();
+        out.nodes4.push_back(igxrt_bvh4_node{});
+        int32_t refs[4] = {0, 0, 0, 0};
+        for (size_t k = 0; k < kids.size(); ++k) {
+            const BNode& c = b.nodes[kids[k]];
+            refs[k] = c.leaf() ? ~(int32_t)leaf_rec[kids[k]] : emit4(kids[k]);
+        }
+        igxrt_bvh4_node& o = out.nodes4[idx];
+        for (int k = 0; k < 4; ++k) {
+            if ((size_t)k < kids.size()) {
+                const Aabb& a = b.nodes[kids[k]].box;
+                o.lo_x[k] = a.lo[0] - pad;
+                o.hi_x[k] = a.hi[0] + pad;
+                o.lo_y[k] = a.lo[1] - pad;
+                o.hi_y[k] = a.hi[1] + pad;
+                o.lo_z[k] = a.lo[2] - pad;
+                o.hi_z[k] = a.hi[2] + pad;
+                o.child[k] = refs[k];
+            } else {
+                o.lo_x[k] = o.hi_x[k] = kInf;
+                o.lo_y[k] = o.hi_y[k] = kInf;
+                o.lo_z[k] = o.hi_z[k] = kInf;
+                o.child[k] = 0;
+            }
+            o.pad[k] = 0;
+        }
+        return (int32_t)idx;
+    }
+
+    void sah(uint32_t id, float root_area) {
+        const BNode& nd = b.nodes[id];
+        const double rel = root_area > 0.f ? (double)nd.box.half_area() / root_area : 1.0;
+        if (nd.leaf()) {
+            sah_tris += rel * nd.count;
+            return;
+        }
+        sah_nodes += rel;
+        sah(nd.left, root_area);
+        sah(nd.right, root_area);
+    }
+};
+
+void empty_slot2(float* x, float* y, float* z) {
+    x[0] = x[1] = y[0] = y[1] = z[0] = z[1] = kInf;
+}
+
+// Largest traversal stack any ray can need: along a root-to-leaf path each
+// node pushes (entered children - 1) entries, at most (non-empty slots - 1).
+uint32_t stack_bound2(const std::vector<igxrt_bvh2_node>& n, int32_t i) {
+    const igxrt_bvh2_node& x = n[i];
+    const bool e1 = x.c1_x[0] == kInf && x.c1_x[1] == kInf;
+    uint32_t deepest = 0;
+    for (int c = 0; c < (e1 ? 1 : 2); ++c)
+        if (x.child[c] >= 0)
+            deepest = std::max(deepest, stack_bound2(n, x.child[c]));
+    return deepest + (e1 ? 0u : 1u);
+}
+
+uint32_t stack_bound4(const std::vector<igxrt_bvh4_node>& n, int32_t i) {
+    const igxrt_bvh4_node& x = n[i];
+    uint32_t deepest = 0, used = 0;
+    for (int c = 0; c < 4; ++c) {
+        if (x.lo_x[c] == kInf && x.hi_x[c] == kInf)
+            continue;
+        ++used;
+        if (x.child[c] >= 0)
+            deepest = std::max(deepest, stack_bound4(n, x.child[c]));
+    }
+    return deepest + (used ? used - 1 : 0);
+}
+
+}  // namespace
+
+igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count, const igxrt_build_options* opts,
+                       igxrt_bvh& out, std::string& err) {
+    out = igxrt_bvh{};
+    if (count > 0 && !tris) {
+        err = "triangles pointer is NULL";
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    }
+    if (count >= 0x7fffffffu) {
+        err = "too many triangles";
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    }
+    Builder b;
+    b.tris = tris;
+    b.n = count;
+    if (opts) {
+        if (opts->max_leaf_size)
+            b.max_leaf = opts->max_leaf_size;
+        if (opts->sah_bins)
+            b.bins = opts->sah_bins;
+        if (opts->node_cost > 0)
+            b.cn = opts->node_cost;
+        if (opts->tri_cost > 0)
+            b.ct = opts->tri_cost;
+    }
+    if (b.max_leaf < 1 || b.max_leaf > 16) {
+        err = format("max_leaf_size %u outside 1..16", b.max_leaf);
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    }
+    if (b.bins < 2 || b.bins > 256) {
+        err = format("sah_bins %u outside 2..256", b.bins);
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    }
+    unsigned hw = std::thread::hardware_concurrency();
+    unsigned threads = (opts && opts->threads) ? opts->threads : (hw ? hw : 1);
+    b.spare_threads = (int)threads - 1;
+
+    out.tris.assign(tris, tris + count);
+    Aabb scene;
+    scene.reset();
+    float maxabs = 0.f;
+    b.tb.resize(count);
+    b.cen.resize(3 * (size_t)count);
+    b.refs.resize(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const igxrt_triangle& t = tris[i];
+        Aabb a;
+        a.reset();
+        const float* v[3] = {t.p0, t.p1, t.p2};
+        for (int k = 0; k < 3; ++k) {
+            for (int c = 0; c < 3; ++c) {
+                if (!std::isfinite(v[k][c])) {
+                    err = format("triangle %u has a non-finite vertex coordinate", i);
+                    out = igxrt_bvh{};
+                    return IGXRT_ERROR_INVALID_ARGUMENT;
+                }
+                maxabs = std::max(maxabs, std::fabs(v[k][c]));
+            }
+            a.grow_point(v[k]);
+        }
+        b.tb[i] = a;
+        for (int c = 0; c < 3; ++c)
+            b.cen[3 * (size_t)i + c] = (a.lo[c] + a.hi[c]) * 0.5f;
+        b.refs[i] = i;
+        scene.grow(a);
+    }
+
+    igxrt_bvh_info& info = out.info;
+    info.triangle_count = count;
+    info.max_leaf_size = b.max_leaf;
+    const float pad = std::max(maxabs * 0x1p-18f, 1e-30f);
+    info.pad_abs = pad;
+    for (int a = 0; a < 3; ++a) {
+        info.bounds[a] = count ? scene.lo[a] : 0.f;
+        info.bounds[3 + a] = count ? scene.hi[a] : 0.f;
+    }
+    if (count == 0)
+        return IGXRT_OK;
+
+    b.nodes.resize(2 * (size_t)count);
+    const uint32_t root = b.build(0, count, 0);
+
+    Layout lay{b, out, pad, std::vector<uint32_t>(b.nodes.size(), 0xffffffffu)};
+    out.prims.reserve(count);
+    const BNode& rn = b.nodes[root];
+    if (rn.leaf()) {
+        // A one-leaf scene still needs a root node: the leaf sits in slot 0.
+        igxrt_bvh2_node n2{};
+        const int32_t ref = lay.emit_leaf(root);
+        lay.set_box(n2.c0_x, n2.c0_y, n2.c0_z, rn.box);
+        empty_slot2(n2.c1_x, n2.c1_y, n2.c1_z);
+        n2.child[0] = ref;
+        n2.child[1] = 0;
+        out.nodes2.push_back(n2);
+        igxrt_bvh4_node n4{};
+        for (int k = 0; k < 4; ++k) {
+            n4.lo_x[k] = n4.hi_x[k] = n4.lo_y[k] = n4.hi_y[k] = n4.lo_z[k] = n4.hi_z[k] = kInf;
+            n4.child[k] = 0;
+        }
+        n4.lo_x[0] = rn.box.lo[0] - pad;
+        n4.hi_x[0] = rn.box.hi[0] + pad;
+        n4.lo_y[0] = rn.box.lo[1] - pad;
+        n4.hi_y[0] = rn.box.hi[1] + pad;
+        n4.lo_z[0] = rn.box.lo[2] - pad;
+        n4.hi_z[0] = rn.box.hi[2] + pad;
+        n4.child[0] = ref;
+        out.nodes4.push_back(n4);
+        lay.max_depth = 1;
+        info.leaf_count = 1;
+    } else {
+        out.nodes2.reserve(count);
+        lay.emit2(root, 1);
+        lay.emit4(root);
+        info.leaf_count = 0;
+        for (const auto& p : out.prims)
+            info.leaf_count += p.leaf_end;
+    }
+    lay.sah(root, rn.box.half_area());
+    info.sah_cost = (float)(b.cn * lay.sah_nodes + b.ct * lay.sah_tris);
+    info.max_depth = lay.max_depth;
+    info.max_stack[IGXRT_LAYOUT_BVH2] = stack_bound2(out.nodes2, 0);
+    info.max_stack[IGXRT_LAYOUT_BVH4] = stack_bound4(out.nodes4, 0);
+    info.bvh2_nodes = (uint32_t)out.nodes2.size();
+    info.bvh4_nodes = (uint32_t)out.nodes4.size();
+    info.device_bytes = sizeof(igxrt_bvh2_node) * out.nodes2.size() +
+                        sizeof(igxrt_bvh4_node) * out.nodes4.size() +
+                        sizeof(igxrt_prim_record) * out.prims.size() +
+                        sizeof(igxrt_triangle) * out.tris.size();
+    return IGXRT_OK;
+}
+
+// ------------------------------------------------------------------------
+// Validation
+// ------------------------------------------------------------------------
+
+namespace {
+
+bool box_empty(float lo, float hi) { return lo == kInf && hi == kInf; }
+
+struct Checker {
+    const igxrt_bvh& b;
+    std::string& msg;
+    std::vector<uint8_t> rec_seen, tri_seen, node_seen;
+
+    bool fail(const std::string& m) {
+        msg = m;
+        return false;
+    }
+
+    bool inside(const float* p, const float lo[3], const float hi[3]) const {
+        for (int a = 0; a < 3; ++a)
+            if (!(p[a] >= lo[a] && p[a] <= hi[a]))
+                return false;
+        return true;
+    }
+
+    bool leaf(int32_t ref, const float lo[3], const float hi[3]) {
+        uint64_t i = (uint32_t)~ref;
+        for (uint32_t k = 0;; ++k, ++i) {
+            if (i >= b.prims.size())
+                return fail(format("leaf record %llu out of range", (unsigned long long)i));
+            if (k >= 16)
+                return fail("leaf longer than 16 records");
+            if (rec_seen[i])
+                return fail(format("primitive record %llu reached twice", (unsigned long long)i));
+            rec_seen[i] = 1;
+            const igxrt_prim_record& r = b.prims[i];
+            if (r.prim >= b.tris.size())
+                return fail(format("record %llu names triangle %u", (unsigned long long)i, r.prim));
+            const igxrt_triangle& t = b.tris[r.prim];
+            for (int a = 0; a < 3; ++a) {
+                const float e1 = t.p1[a] - t.p0[a], e2 = t.p2[a] - t.p0[a];
+                if (memcmp(&r.p0[a], &t.p0[a], 4) || memcmp(&r.e1[a], &e1, 4) ||
+                    memcmp(&r.e2[a], &e2, 4))
+                    return fail(format("record %llu does not match triangle %u",
+                                       (unsigned long long)i, r.prim));
+            }
+            if (!inside(t.p0, lo, hi) || !inside(t.p1, lo, hi) || !inside(t.p2, lo, hi))
+                return fail(format("triangle %u outside its leaf box", r.prim));
+            if (r.leaf_end)
+                break;
+        }
+        return true;
+    }
+};
+
+}  // namespace
+
+igxrt_status validate_bvh(const igxrt_bvh& b, std::string& msg) {
+    const size_t nt = b.tris.size();
+    if (b.prims.size() != nt) {
+        msg = format("%zu primitive records for %zu triangles", b.prims.size(), nt);
+        return IGXRT_ERROR_INVALID_BVH;
+    }
+    if (nt == 0) {
+        if (!b.nodes2.empty() || !b.nodes4.empty()) {
+            msg = "empty scene with nodes";
+            return IGXRT_ERROR_INVALID_BVH;
+        }
+        return IGXRT_OK;
+    }
+    if (b.nodes2.empty() || b.nodes4.empty()) {
+        msg = "non-empty scene without nodes";
+        return IGXRT_ERROR_INVALID_BVH;
+    }
+    for (uint32_t l = 0; l < IGXRT_LAYOUT_COUNT; ++l)
+        if (b.info.max_stack[l] > kStackCapacity) {
+            msg = format("layout %u needs a %u-entry stack (limit %u)", l, b.info.max_stack[l],
+                         kStackCapacity);
+            return IGXRT_ERROR_INVALID_BVH;
+        }
+    for (int layout = 0; layout < 2; ++layout) {
+        Checker ck{b, msg, std::vector<uint8_t>(nt, 0), std::vector<uint8_t>(nt, 0), {}};
+        const size_t nn = layout == 0 ? b.nodes2.size() : b.nodes4.size();
+        ck.node_seen.assign(nn, 0);
+        struct Item {
+            int32_t node;
+            uint32_t depth;
+        };
+        std::vector<Item> stack = {{0, 1}};
+        while (!stack.empty()) {
+            const Item it = stack.back();
+            stack.pop_back();
+            if (it.node < 0 || (size_t)it.node >= nn) {
+                msg = format("node index %d out of range", it.node);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+            if (ck.node_seen[it.node]) {
+                msg = format("node %d reached twice", it.node);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+            ck.node_seen[it.node] = 1;
+            if (it.depth > kMaxDepth) {
+                msg = format("depth %u exceeds %u", it.depth, kMaxDepth);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+            const int slots = layout == 0 ? 2 : 4;
+            for (int c = 0; c < slots; ++c) {
+                float lo[3], hi[3];
+                int32_t ref;
+                if (layout == 0) {
+                    const igxrt_bvh2_node& n = b.nodes2[it.node];
+                    const float* x = c ? n.c1_x : n.c0_x;
+                    const float* y = c ? n.c1_y : n.c0_y;
+                    const float* z = c ? n.c1_z : n.c0_z;
+                    lo[0] = x[0]; hi[0] = x[1];
+                    lo[1] = y[0]; hi[1] = y[1];
+                    lo[2] = z[0]; hi[2] = z[1];
+                    ref = n.child[c];
+                } else {
+                    const igxrt_bvh4_node& n = b.nodes4[it.node];
+                    lo[0] = n.lo_x[c]; hi[0] = n.hi_x[c];
+                    lo[1] = n.lo_y[c]; hi[1] = n.hi_y[c];
+                    lo[2] = n.lo_z[c]; hi[2] = n.hi_z[c];
+                    ref = n.child[c];
+                }
+                if (box_empty(lo[0], hi[0]) && box_empty(lo[1], hi[1]) && box_empty(lo[2], hi[2]))
+                    continue;
+                if (ref < 0) {
+                    if (!ck.leaf(ref, lo, hi))
+                        return IGXRT_ERROR_INVALID_BVH;
+                } else {
+                    // Interior child: its own child boxes must lie inside this box.
+                    if ((size_t)ref >= nn) {
+                        msg = format("child index %d out of range", ref);
+                        return IGXRT_ERROR_INVALID_BVH;
+                    }
+                    const int sub = layout == 0 ? 2 : 4;
+                    for (int g = 0; g < sub; ++g) {
+                        float glo[3], ghi[3];
+                        if (layout == 0) {
+                            const igxrt_bvh2_node& m = b.nodes2[ref];
+                            const float* x = g ? m.c1_x : m.c0_x;
+                            const float* y = g ? m.c1_y : m.c0_y;
+                            const float* z = g ? m.c1_z : m.c0_z;
+                            glo[0] = x[0]; ghi[0] = x[1];
+                            glo[1] = y[0]; ghi[1] = y[1];
+                            glo[2] = z[0]; ghi[2] = z[1];
+                        } else {
+                            const igxrt_bvh4_node& m = b.nodes4[ref];
+                            glo[0] = m.lo_x[g]; ghi[0] = m.hi_x[g];
+                            glo[1] = m.lo_y[g]; ghi[1] = m.hi_y[g];
+                            glo[2] = m.lo_z[g]; ghi[2] = m.hi_z[g];
+                        }
+                        if (box_empty(glo[0], ghi[0]))
+                            continue;
+                        for (int a = 0; a < 3; ++a)
+                            if (!(glo[a] >= lo[a] && ghi[a] <= hi[a])) {
+                                msg = format("node %d child box escapes its parent box", ref);
+                                return IGXRT_ERROR_INVALID_BVH;
+                            }
+                    }
+                    stack.push_back({ref, it.depth + 1});
+                }
+            }
+        }
+        for (size_t i = 0; i < nn; ++i)
+            if (!ck.node_seen[i]) {
+                msg = format("node %zu unreachable", i);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+        for (size_t i = 0; i < nt; ++i) {
+            if (!ck.rec_seen[i]) {
+                msg = format("primitive record %zu unreachable", i);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+        }
+        std::vector<uint8_t> tri_seen(nt, 0);
+        for (const auto& r : b.prims) {
+            if (tri_seen[r.prim]) {
+                msg = format("triangle %u in two leaves", r.prim);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+            tri_seen[r.prim] = 1;
+        }
+    }
+    return IGXRT_OK;
+}
+
+}  // namespace igxrt
+
+// ------------------------------------------------------------------------
+// C ABI: host BVH objects
+// ------------------------------------------------------------------------
+
+using namespace igxrt;
+
+namespace {
+
+struct FileHeader {
+    char magic[8];
+    uint32_t version;
+    uint32_t abi;
+    uint64_t tris, nodes2, nodes4, prims;
+    igxrt_bvh_info info;
+};
+
+constexpr char kMagic[8] = {'I', 'G', 'X', 'R', 'T', 'B', 'V', 'H'};
+
+}  // namespace
+
+extern "C" {
+
+igxrt_status igxrt_bvh_build(const igxrt_triangle* tris, uint32_t count,
+                             const igxrt_build_options* opts, igxrt_bvh** out) {
+    if (!out)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    igxrt_bvh* b = new (std::nothrow) igxrt_bvh();
+    if (!b)
+        return IGXRT_ERROR_OUT_OF_MEMORY;
+    std::string err;
+    igxrt_status st;
+    try {
+        st = build_bvh(tris, count, opts, *b, err);
+    } catch (const std::bad_alloc&) {
+        st = IGXRT_ERROR_OUT_OF_MEMORY;
+    }
+    if (st != IGXRT_OK) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_bvh_destroy(igxrt_bvh* bvh) {
+    delete bvh;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_bvh_get_info(const igxrt_bvh* bvh, igxrt_bvh_info* info) {
+    if (!bvh || !info)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *info = bvh->info;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_bvh_get_data(const igxrt_bvh* bvh, uint32_t layout, const void** nodes,
+                                uint64_t* node_count, const igxrt_prim_record** prims,
+                                uint64_t* prim_count) {
+    if (!bvh || layout >= IGXRT_LAYOUT_COUNT)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    if (nodes)
+        *nodes = layout == IGXRT_LAYOUT_BVH2 ? (const void*)bvh->nodes2.data()
+                                             : (const void*)bvh->nodes4.data();
+    if (node_count)
+        *node_count = layout == IGXRT_LAYOUT_BVH2 ? bvh->nodes2.size() : bvh->nodes4.size();
+    if (prims)
+        *prims = bvh->prims.data();
+    if (prim_count)
+        *prim_count = bvh->prims.size();
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_bvh_validate(const igxrt_bvh* bvh, char* msg, size_t msg_len) {
+    if (!bvh)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    std::string m;
+    const igxrt_status st = validate_bvh(*bvh, m);
+    if (msg && msg_len) {
+        snprintf(msg, msg_len, "%s", st == IGXRT_OK ? "ok" : m.c_str());
+    }
+    return st;
+}
+
+igxrt_status igxrt_bvh_save(const igxrt_bvh* bvh, const char* path) {
+    if (!bvh || !path)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    FILE* f = fopen(path, "wb");
+    if (!f)
+        return IGXRT_ERROR_IO;
+    FileHeader h{};
+    memcpy(h.magic, kMagic, 8);
+    h.version = 1;
+    h.abi = IGXRT_ABI_VERSION;
+    h.tris = bvh->tris.size();
+    h.nodes2 = bvh->nodes2.size();
+    h.nodes4 = bvh->nodes4.size();
+    h.prims = bvh->prims.size();
+    h.info = bvh->info;
+    bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+    ok = ok && fwrite(bvh->tris.data(), sizeof(igxrt_triangle), h.tris, f) == h.tris;
+    ok = ok && fwrite(bvh->nodes2.data(), sizeof(igxrt_bvh2_node), h.nodes2, f) == h.nodes2;
+    ok = ok && fwrite(bvh->nodes4.data(), sizeof(igxrt_bvh4_node), h.nodes4, f) == h.nodes4;
+    ok = ok && fwrite(bvh->prims.data(), sizeof(igxrt_prim_record), h.prims, f) == h.prims;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? IGXRT_OK : IGXRT_ERROR_IO;
+}
+
+igxrt_status igxrt_bvh_load(const char* path, igxrt_bvh** out) {
+    if (!path || !out)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    FILE* f = fopen(path, "rb");
+    if (!f)
+        return IGXRT_ERROR_IO;
+    FileHeader h{};
+    igxrt_bvh* b = nullptr;
+    igxrt_status st = IGXRT_ERROR_IO;
+    do {
+        if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, kMagic, 8) || h.version != 1)
+            break;
+        if (h.tris >= 0x7fffffffu || h.prims != h.tris || h.nodes2 > 2 * h.tris + 1 ||
+            h.nodes4 > 2 * h.tris + 1)
+            break;
+        b = new (std::nothrow) igxrt_bvh();
+        if (!b) {
+            st = IGXRT_ERROR_OUT_OF_MEMORY;
+            break;
+        }
+        b->tris.resize(h.tris);
+        b->nodes2.resize(h.nodes2);
+        b->nodes4.resize(h.nodes4);
+        b->prims.resize(h.prims);
+        if (fread(b->tris.data(), sizeof(igxrt_triangle), h.tris, f) != h.tris ||
+            fread(b->nodes2.data(), sizeof(igxrt_bvh2_node), h.nodes2, f) != h.nodes2 ||
+            fread(b->nodes4.data(), sizeof(igxrt_bvh4_node), h.nodes4, f) != h.nodes4 ||
+            fread(b->prims.data(), sizeof(igxrt_prim_record), h.prims, f) != h.prims)
+            break;
+        b->info = h.info;
+        std::string m;
+        st = validate_bvh(*b, m);
+    } while (false);
+    fclose(f);
+    if (st != IGXRT_OK) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return IGXRT_OK;
+}
+
+}  // extern "C"

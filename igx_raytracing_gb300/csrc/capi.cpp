@@ -1,0 +1,476 @@
+// capi.cpp — C ABI: contexts, resident scenes and ray-query entry points.
+//
+// Replaces the reference's dispatch boundary: RaygenTask / ShadowTask bind the
+// SceneGraph's scene buffers and Dispatch a compute shader
+// (src/rt/task/raygen_task.cpp:88-94, src/rt/task/shadow_task.cpp:194-213);
+// here a scene is uploaded once (igxrt_scene_create) and each query is one
+// stream-ordered call (igxrt_trace_closest / igxrt_trace_any).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+
+namespace igxrt {
+
+igxrt_status fail(igxrt_context* ctx, igxrt_status st, const std::string& msg) {
+    if (ctx)
+        ctx->last_error = msg;
+    return st;
+}
+
+igxrt_status cuda_fail(igxrt_context* ctx, cudaError_t e, const char* what) {
+    const igxrt_status st = e == cudaErrorMemoryAllocation ? IGXRT_ERROR_OUT_OF_MEMORY : IGXRT_ERROR_CUDA;
+    return fail(ctx, st, format("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e)));
+}
+
+DeviceGuard::DeviceGuard(int device) {
+    if (cudaGetDevice(&prev_) != cudaSuccess)
+        prev_ = -1;
+    ok_ = (prev_ == device) || cudaSetDevice(device) == cudaSuccess;
+}
+
+DeviceGuard::~DeviceGuard() {
+    int cur = -1;
+    if (prev_ >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev_)
+        cudaSetDevice(prev_);
+}
+
+uint32_t* take_queue_slot(igxrt_context* ctx) {
+    const uint32_t s = ctx->next_slot;
+    ctx->next_slot = (s + 1) % kQueueSlots;
+    return ctx->d_words + s;
+}
+
+uint32_t* status_word(igxrt_context* ctx) { return ctx->d_words + kQueueSlots; }
+
+igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, igxrt_launch_params& out) {
+    out = in;
+    if (!out.block_size)
+        out.block_size = 128;
+    if (!out.packet_size)
+        out.packet_size = 64;
+    if (out.stack_depth == 0 && in.block_size == 0 && in.packet_size == 0)
+        out.stack_depth = 16;
+    if (out.block_size < 32 || out.block_size > 256 || out.block_size % 32)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    format("block_size %u: use a multiple of 32 up to 256", out.block_size));
+    if (out.packet_size < 32 || out.packet_size > 4096 || out.packet_size % 32)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    format("packet_size %u: use a multiple of 32 up to 4096", out.packet_size));
+    if (out.stack_depth > 64)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    format("stack_depth %u: at most 64 shared entries", out.stack_depth));
+    if (out.layout >= IGXRT_LAYOUT_COUNT)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown layout %u", out.layout));
+    return IGXRT_OK;
+}
+
+}  // namespace igxrt
+
+using namespace igxrt;
+
+namespace {
+
+bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Rejects host pointers passed without IGXRT_TRACE_HOST_MEMORY: a kernel
+// would fault on them.
+bool device_accessible(const void* p) {
+    if (!p)
+        return true;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged ||
+           (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr);
+}
+
+igxrt_status check_scene(igxrt_context* ctx, const igxrt_scene* scene) {
+    if (!scene)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "scene is NULL");
+    if (scene->device != ctx->device)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    format("scene lives on device %d, context on %d", scene->device, ctx->device));
+    return IGXRT_OK;
+}
+
+igxrt_status grow_stage(igxrt_context* ctx, size_t bytes) {
+    if (ctx->stage_bytes >= bytes)
+        return IGXRT_OK;
+    if (ctx->d_stage) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "staging resize");
+        cudaFree(ctx->d_stage);
+        ctx->d_stage = nullptr;
+        ctx->stage_bytes = 0;
+    }
+    size_t want = std::max(bytes, ctx->stage_bytes * 2);
+    cudaError_t e = cudaMalloc(&ctx->d_stage, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        e = cudaMalloc(&ctx->d_stage, bytes);
+        want = bytes;
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "staging allocation");
+    ctx->stage_bytes = want;
+    return IGXRT_OK;
+}
+
+size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+igxrt_status read_status(igxrt_context* ctx) {
+    uint32_t word = 0;
+    cudaError_t e = cudaMemcpy(&word, status_word(ctx), sizeof(word), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "status read");
+    if (word) {
+        cudaMemset(status_word(ctx), 0, sizeof(uint32_t));
+        return fail(ctx, IGXRT_ERROR_KERNEL_STATUS,
+                    format("kernel error word 0x%x (1 = traversal stack overflow)", word));
+    }
+    return IGXRT_OK;
+}
+
+igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_ray* rays,
+                          const uint32_t* prev, uint32_t count, uint32_t mode, void* out,
+                          uint32_t flags, void* stream_ptr, uint32_t* nf, uint32_t* pf,
+                          const igxrt_launch_params& params) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    igxrt_status st = check_scene(ctx, scene);
+    if (st != IGXRT_OK)
+        return st;
+    if (count == 0)
+        return IGXRT_OK;
+    if (count > 0x7fffffffu)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "more than 2^31-1 rays in one call");
+    if (!rays || !out)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "rays and output must be non-NULL");
+    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    if (!aligned(rays, 16) || (mode == 0 && !aligned(out, 16)) || !aligned(out, 4) ||
+        !aligned(prev, 4) || !aligned(nf, 4) || !aligned(pf, 4))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    "rays and hits must be 16-byte aligned, other arrays 4-byte aligned");
+    igxrt_launch_params p;
+    st = resolve_params(ctx, params, p);
+    if (st != IGXRT_OK)
+        return st;
+    DeviceGuard guard(ctx->device);
+    if (!guard.ok())
+        return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    const size_t out_elem = mode == 0 ? sizeof(igxrt_hit) : sizeof(uint32_t);
+
+    if (!(flags & IGXRT_TRACE_HOST_MEMORY)) {
+        if (!device_accessible(rays) || !device_accessible(prev) || !device_accessible(out) ||
+            !device_accessible(nf) || !device_accessible(pf))
+            return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                        "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
+        TraceRequest req{scene, rays, prev, count, mode, mode == 0 ? (igxrt_hit*)out : nullptr,
+                         mode == 1 ? (uint32_t*)out : nullptr, nf, pf};
+        return launch_trace(ctx, req, p, stream);
+    }
+
+    // Host arrays: stage through the context's device buffer.
+    const size_t rb = round_up((size_t)count * sizeof(igxrt_ray), 256);
+    const size_t pb = prev ? round_up((size_t)count * 4, 256) : 0;
+    const size_t ob = round_up((size_t)count * out_elem, 256);
+    const size_t cb = nf ? 2 * round_up((size_t)count * 4, 256) : 0;
+    st = grow_stage(ctx, rb + pb + ob + cb);
+    if (st != IGXRT_OK)
+        return st;
+    char* base = (char*)ctx->d_stage;
+    igxrt_ray* d_rays = (igxrt_ray*)base;
+    uint32_t* d_prev = prev ? (uint32_t*)(base + rb) : nullptr;
+    void* d_out = base + rb + pb;
+    uint32_t* d_nf = nf ? (uint32_t*)(base + rb + pb + ob) : nullptr;
+    uint32_t* d_pf = nf ? (uint32_t*)(base + rb + pb + ob + cb / 2) : nullptr;
+    cudaError_t e = cudaMemcpyAsync(d_rays, rays, (size_t)count * sizeof(igxrt_ray),
+                                    cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess && prev)
+        e = cudaMemcpyAsync(d_prev, prev, (size_t)count * 4, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "ray upload");
+    TraceRequest req{scene, d_rays, d_prev, count, mode, mode == 0 ? (igxrt_hit*)d_out : nullptr,
+                     mode == 1 ? (uint32_t*)d_out : nullptr, d_nf, d_pf};
+    st = launch_trace(ctx, req, p, stream);
+    if (st != IGXRT_OK)
+        return st;
+    e = cudaMemcpyAsync(out, d_out, (size_t)count * out_elem, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess && nf) {
+        e = cudaMemcpyAsync(nf, d_nf, (size_t)count * 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(pf, d_pf, (size_t)count * 4, cudaMemcpyDeviceToHost, stream);
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "result download");
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "trace");
+    return read_status(ctx);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* igxrt_status_string(igxrt_status s) {
+    switch (s) {
+        case IGXRT_OK: return "ok";
+        case IGXRT_ERROR_INVALID_ARGUMENT: return "invalid argument";
+        case IGXRT_ERROR_CUDA: return "CUDA error";
+        case IGXRT_ERROR_OUT_OF_MEMORY: return "out of memory";
+        case IGXRT_ERROR_INVALID_BVH: return "invalid BVH";
+        case IGXRT_ERROR_KERNEL_STATUS: return "kernel raised its error word";
+        case IGXRT_ERROR_ADMISSION: return "request exceeds the admission cap";
+        case IGXRT_ERROR_TIMEOUT: return "timed out";
+        case IGXRT_ERROR_UNSUPPORTED: return "unsupported";
+        case IGXRT_ERROR_NOT_READY: return "not ready";
+        case IGXRT_ERROR_IO: return "I/O error";
+    }
+    return "unknown status";
+}
+
+igxrt_status igxrt_create(int device, igxrt_context** out) {
+    if (!out)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return IGXRT_ERROR_CUDA;
+    }
+    if (device < 0 || device >= n)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    DeviceGuard guard(device);
+    if (!guard.ok())
+        return IGXRT_ERROR_CUDA;
+    igxrt_context* ctx = new (std::nothrow) igxrt_context();
+    if (!ctx)
+        return IGXRT_ERROR_OUT_OF_MEMORY;
+    ctx->device = device;
+    if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaMalloc(&ctx->d_words, (kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(ctx->d_words, 0, (kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        if (ctx->d_words)
+            cudaFree(ctx->d_words);
+        delete ctx;
+        return IGXRT_ERROR_CUDA;
+    }
+    igxrt_launch_params defaults{};
+    resolve_params(ctx, defaults, ctx->params);
+    *out = ctx;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_destroy(igxrt_context* ctx) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    {
+        DeviceGuard guard(ctx->device);
+        cudaDeviceSynchronize();
+        if (ctx->d_stage)
+            cudaFree(ctx->d_stage);
+        if (ctx->d_words)
+            cudaFree(ctx->d_words);
+    }
+    delete ctx;
+    return IGXRT_OK;
+}
+
+const char* igxrt_last_error(const igxrt_context* ctx) {
+    if (!ctx)
+        return "context is NULL";
+    return ctx->last_error.c_str();
+}
+
+igxrt_status igxrt_set_launch_params(igxrt_context* ctx, const igxrt_launch_params* p) {
+    if (!ctx || !p)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    igxrt_launch_params r;
+    const igxrt_status st = resolve_params(ctx, *p, r);
+    if (st == IGXRT_OK)
+        ctx->params = r;
+    return st;
+}
+
+igxrt_status igxrt_get_launch_params(const igxrt_context* ctx, igxrt_launch_params* p) {
+    if (!ctx || !p)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *p = ctx->params;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bvh, igxrt_scene** out) {
+    if (!ctx || !bvh || !out)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    DeviceGuard guard(ctx->device);
+    if (!guard.ok())
+        return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
+    igxrt_scene* s = new (std::nothrow) igxrt_scene();
+    if (!s)
+        return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "scene object");
+    s->device = ctx->device;
+    s->info = bvh->info;
+    const size_t b2 = round_up(bvh->nodes2.size() * sizeof(igxrt_bvh2_node), 256);
+    const size_t b4 = round_up(bvh->nodes4.size() * sizeof(igxrt_bvh4_node), 256);
+    const size_t bp = round_up(bvh->prims.size() * sizeof(igxrt_prim_record), 256);
+    const size_t bt = round_up(bvh->tris.size() * sizeof(igxrt_triangle), 256);
+    const size_t total = std::max<size_t>(b2 + b4 + bp + bt, 256);
+    cudaError_t e = cudaMalloc(&s->d_mem, total);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_fail(ctx, e, "scene allocation");
+    }
+    char* base = (char*)s->d_mem;
+    s->nodes[IGXRT_LAYOUT_BVH2] = base;
+    s->nodes[IGXRT_LAYOUT_BVH4] = base + b2;
+    s->prims = (const igxrt_prim_record*)(base + b2 + b4);
+    s->tris = (const igxrt_triangle*)(base + b2 + b4 + bp);
+    s->node_count[IGXRT_LAYOUT_BVH2] = (uint32_t)bvh->nodes2.size();
+    s->node_count[IGXRT_LAYOUT_BVH4] = (uint32_t)bvh->nodes4.size();
+    if (!bvh->nodes2.empty())
+        e = cudaMemcpy(base, bvh->nodes2.data(), bvh->nodes2.size() * sizeof(igxrt_bvh2_node), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !bvh->nodes4.empty())
+        e = cudaMemcpy(base + b2, bvh->nodes4.data(), bvh->nodes4.size() * sizeof(igxrt_bvh4_node), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !bvh->prims.empty())
+        e = cudaMemcpy(base + b2 + b4, bvh->prims.data(), bvh->prims.size() * sizeof(igxrt_prim_record), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !bvh->tris.empty())
+        e = cudaMemcpy(base + b2 + b4 + bp, bvh->tris.data(), bvh->tris.size() * sizeof(igxrt_triangle), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(s->d_mem);
+        delete s;
+        return cuda_fail(ctx, e, "scene upload");
+    }
+    *out = s;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_scene_create(igxrt_context* ctx, const igxrt_triangle* tris, uint32_t count,
+                                const igxrt_build_options* opts, igxrt_scene** out) {
+    if (!ctx || !out)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    igxrt_bvh bvh;
+    std::string err;
+    igxrt_status st;
+    try {
+        st = build_bvh(tris, count, opts, bvh, err);
+    } catch (const std::bad_alloc&) {
+        st = IGXRT_ERROR_OUT_OF_MEMORY;
+        err = "host memory exhausted during the BVH build";
+    }
+    if (st != IGXRT_OK)
+        return fail(ctx, st, err);
+    return igxrt_scene_create_from_bvh(ctx, &bvh, out);
+}
+
+igxrt_status igxrt_scene_destroy(igxrt_scene* scene) {
+    if (!scene)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    {
+        DeviceGuard guard(scene->device);
+        cudaDeviceSynchronize();
+        cudaFree(scene->d_mem);
+    }
+    delete scene;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info) {
+    if (!scene || !info)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *info = scene->info;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_trace_closest(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_ray* rays,
+                                 const uint32_t* prev_hit, uint32_t count, igxrt_hit* hits,
+                                 uint32_t flags, void* stream) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    return trace_common(ctx, scene, rays, prev_hit, count, 0, hits, flags, stream, nullptr, nullptr,
+                        ctx->params);
+}
+
+igxrt_status igxrt_trace_any(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_ray* rays,
+                             const uint32_t* prev_hit, uint32_t count, uint32_t* occluded,
+                             uint32_t flags, void* stream) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    return trace_common(ctx, scene, rays, prev_hit, count, 1, occluded, flags, stream, nullptr,
+                        nullptr, ctx->params);
+}
+
+igxrt_status igxrt_count_fetches(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_ray* rays,
+                                 const uint32_t* prev_hit, uint32_t count, uint32_t mode,
+                                 uint32_t layout, uint32_t* node_fetches, uint32_t* prim_fetches,
+                                 void* stream) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    if (mode > 1 || layout >= IGXRT_LAYOUT_COUNT || !node_fetches || !prim_fetches)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "mode 0/1, a valid layout and both count arrays");
+    if (count == 0)
+        return IGXRT_OK;
+    // The instrumented kernel also writes the query's results; they go to a
+    // scratch area inside the staging buffer.
+    igxrt_launch_params p = ctx->params;
+    p.layout = layout;
+    DeviceGuard guard(ctx->device);
+    cudaPointerAttributes attr;
+    const bool host = cudaPointerGetAttributes(&attr, node_fetches) != cudaSuccess ||
+                      attr.type == cudaMemoryTypeUnregistered;
+    cudaGetLastError();
+    const size_t ob = round_up((size_t)count * (mode == 0 ? sizeof(igxrt_hit) : 4), 256);
+    if (host) {
+        // Host count arrays: the results buffer is host memory too.
+        std::vector<char> scratch_out(ob);
+        return trace_common(ctx, scene, rays, prev_hit, count, mode, scratch_out.data(),
+                            IGXRT_TRACE_HOST_MEMORY, stream, node_fetches, prim_fetches, p);
+    }
+    void* d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_out, ob);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "count scratch");
+    const igxrt_status st = trace_common(ctx, scene, rays, prev_hit, count, mode, d_out, 0, stream,
+                                         node_fetches, prim_fetches, p);
+    cudaStreamSynchronize((cudaStream_t)stream);
+    cudaFree(d_out);
+    return st;
+}
+
+igxrt_status igxrt_fetch_hits(igxrt_context* ctx, const igxrt_hit* device_hits, uint32_t count,
+                              igxrt_hit* host_hits, void* stream) {
+    if (!ctx || (count && (!device_hits || !host_hits)))
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    DeviceGuard guard(ctx->device);
+    cudaError_t e = cudaMemcpyAsync(host_hits, device_hits, (size_t)count * sizeof(igxrt_hit),
+                                    cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "fetch hits");
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_sync(igxrt_context* ctx, void* stream) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    DeviceGuard guard(ctx->device);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "stream synchronize");
+    return read_status(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// trace_kernels.cu — the plain traversal kernels and their launcher.
+//
+// One persistent kernel per (node layout, query mode, instrumentation):
+// CTAs stay resident, each warp repeatedly takes a packet of `packet` rays
+// from a global atomic work queue and its lanes trace them, so uneven ray
+// costs (a miss of the root box vs. a deep closest hit) balance across the
+// GPU without a tail of idle SMs.  Node and primitive records are read with
+// 128-bit read-only loads; hit records are written with streaming stores so
+// they do not displace BVH lines from L2.
+#include <algorithm>
+
+#include "engine.h"
+#include "traverse.cuh"
+
+namespace igxrt {
+
+static_assert(kStackCapacityDevice == kStackCapacity, "stack capacity mismatch");
+static_assert(sizeof(igxrt_bvh2_node) == 64, "BVH2 node must be 64 bytes");
+static_assert(sizeof(igxrt_bvh4_node) == 128, "BVH4 node must be 128 bytes");
+static_assert(sizeof(igxrt_prim_record) == 48, "primitive record must be 48 bytes");
+static_assert(sizeof(igxrt_ray) == 32, "ray must be 32 bytes");
+static_assert(sizeof(igxrt_hit) == 16, "hit must be 16 bytes");
+
+struct KernelArgs {
+    const float4* nodes;
+    const float4* prims;
+    uint32_t node_count;
+    const igxrt_ray* rays;
+    const uint32_t* prev;
+    uint32_t count;
+    igxrt_hit* hits;
+    uint32_t* occluded;
+    uint32_t* node_fetches;
+    uint32_t* prim_fetches;
+    uint32_t* queue;
+    uint32_t* status;
+    uint32_t packet;
+    uint32_t sh_depth;
+};
+
+template <int LAYOUT, bool ANY, bool COUNT>
+__device__ __forceinline__ void trace_ray(const KernelArgs& a, uint32_t i, TraversalStack& st) {
+    const uint32_t prev = a.prev ? __ldg(a.prev + i) : IGXRT_NO_RAY_HIT;
+    const RayState r = load_ray(a.rays, i, prev);
+    BestHit best;
+    best.t = r.tmax_eff;
+    best.u = 0.f;
+    best.v = 0.f;
+    best.prim = 0;  // "prim < best.prim" cannot hold before a first hit
+    best.tcull = cull_limit(best.t);
+    bool occluded = false, ok = true;
+    uint32_t nf = 0, pf = 0;
+    st.sp = 0;
+    if (a.node_count) {
+        if (LAYOUT == IGXRT_LAYOUT_BVH4)
+            ok = traverse_bvh4<ANY, COUNT>(a.nodes, a.prims, r, best, st, occluded, nf, pf);
+        else
+            ok = traverse_bvh2<ANY, COUNT>(a.nodes, a.prims, r, best, st, occluded, nf, pf);
+    }
+    if (!ok)
+        atomicOr(a.status, kStatusStackOverflow);
+    if (ANY) {
+        __stcs(a.occluded + i, occluded ? 1u : 0u);
+    } else {
+        const bool hit = best.t < r.tmax_eff;
+        const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(best.prim))
+                             : make_float4(IGXRT_NO_HIT, 0.f, 0.f, __uint_as_float(IGXRT_NO_RAY_HIT));
+        __stcs(reinterpret_cast<float4*>(a.hits) + i, h);
+    }
+    if (COUNT) {
+        a.node_fetches[i] = nf;
+        a.prim_fetches[i] = pf;
+    }
+}
+
+template <int LAYOUT, bool ANY, bool COUNT>
+__global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
+    extern __shared__ uint32_t smem[];
+    TraversalStack st;
+    st.sh = smem + threadIdx.x;
+    st.stride = blockDim.x;
+    st.sh_depth = a.sh_depth;
+    st.sp = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0)
+            base = atomicAdd(a.queue, a.packet);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= a.count)
+            break;
+        const uint32_t end = min(base + a.packet, a.count);
+        for (uint32_t i = base + lane; i < end; i += 32)
+            trace_ray<LAYOUT, ANY, COUNT>(a, i, st);
+    }
+}
+
+using KernelFn = void (*)(KernelArgs);
+
+static KernelFn select_kernel(uint32_t layout, bool any, bool count) {
+    if (layout == IGXRT_LAYOUT_BVH4) {
+        if (count)
+            return any ? trace_kernel<IGXRT_LAYOUT_BVH4, true, true> : trace_kernel<IGXRT_LAYOUT_BVH4, false, true>;
+        return any ? trace_kernel<IGXRT_LAYOUT_BVH4, true, false> : trace_kernel<IGXRT_LAYOUT_BVH4, false, false>;
+    }
+    if (count)
+        return any ? trace_kernel<IGXRT_LAYOUT_BVH2, true, true> : trace_kernel<IGXRT_LAYOUT_BVH2, false, true>;
+    return any ? trace_kernel<IGXRT_LAYOUT_BVH2, true, false> : trace_kernel<IGXRT_LAYOUT_BVH2, false, false>;
+}
+
+igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
+                          const igxrt_launch_params& p, cudaStream_t stream) {
+    if (req.count == 0)
+        return IGXRT_OK;
+    const igxrt_scene* s = req.scene;
+    const bool count = req.node_fetches != nullptr;
+    KernelFn fn = select_kernel(p.layout, req.mode == 1, count);
+    const size_t smem = (size_t)p.stack_depth * p.block_size * sizeof(uint32_t);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "occupancy query");
+    if (per_sm < 1)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "launch parameters leave no resident CTA");
+    if (p.ctas_per_sm)
+        per_sm = std::min(per_sm, (int)p.ctas_per_sm);
+    const uint64_t warps_needed = ((uint64_t)req.count + p.packet_size - 1) / p.packet_size;
+    const uint64_t ctas_needed = (warps_needed + p.block_size / 32 - 1) / (p.block_size / 32);
+    const uint32_t grid = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, ctas_needed));
+
+    KernelArgs a;
+    a.nodes = reinterpret_cast<const float4*>(s->nodes[p.layout]);
+    a.prims = reinterpret_cast<const float4*>(s->prims);
+    a.node_count = s->node_count[p.layout];
+    a.rays = req.rays;
+    a.prev = req.prev;
+    a.count = req.count;
+    a.hits = req.hits;
+    a.occluded = req.occluded;
+    a.node_fetches = req.node_fetches;
+    a.prim_fetches = req.prim_fetches;
+    a.queue = take_queue_slot(ctx);
+    a.status = status_word(ctx);
+    a.packet = p.packet_size;
+    a.sh_depth = p.stack_depth;
+    e = cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "queue reset");
+    fn<<<grid, p.block_size, smem, stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "trace kernel launch");
+    return IGXRT_OK;
+}
+
+}  // namespace igxrt

@@ -1,0 +1,303 @@
+// traverse.cuh — device-side ray/box and ray/triangle tests and the BVH
+// traversal loops shared by the plain, batched and instrumented kernels.
+//
+// Arithmetic contract (identical to the host oracle in oracle/trace_oracle.c):
+//   * the triangle test is rayIntersectTri (res/shaders/primitive.glsl:239-284)
+//     in binary32 with every multiply and add rounded separately
+//     (__fmul_rn / __fadd_rn / __fsub_rn never fuse), dot products summed left
+//     to right, cross products in GLSL component order, f = 1/a correctly
+//     rounded (__frcp_rn), denormals kept (the library is built without
+//     -ftz);
+//   * the slab test uses explicit fmaf on both sides so the host and the GPU
+//     cull the same boxes and visit nodes in the same order;
+//   * a hit (t, prim) replaces the best one when t < best.t, or t == best.t
+//     and prim < best.prim: the linear loop's "first index reaching the
+//     smallest t" (trace.glsl:25-27 with the strict t >= hit.hitT rejection at
+//     primitive.glsl:276), independent of visiting order.
+#pragma once
+
+#include <cstdint>
+
+#include "igxrt.h"
+
+namespace igxrt {
+
+constexpr uint32_t kStatusStackOverflow = 1u;
+// Traversal stack entries per ray (shared part + local spill).
+constexpr uint32_t kStackCapacityDevice = 128;
+
+struct RayState {
+    float ox, oy, oz;
+    float dx, dy, dz;
+    float ix, iy, iz;     // 1/d with |d| < 2^-80 raised to 2^-80
+    float oix, oiy, oiz;  // o * (1/d)
+    float tmin, tmin_box, tmax_eff;
+    uint32_t prev;
+};
+
+struct BestHit {
+    float t, u, v;
+    uint32_t prim;
+    float tcull;
+};
+
+__device__ __forceinline__ float safe_dir(float d) {
+    return fabsf(d) < 0x1p-80f ? copysignf(0x1p-80f, d) : d;
+}
+
+// Upper bound used to cull boxes: best t widened by 2^-10 (relative), kept
+// finite so the {+inf} box of an absent child is never entered.
+__device__ __forceinline__ float cull_limit(float t) {
+    return fminf(__fmaf_rn(t, 0x1p-10f, t), 3.4028235e38f);
+}
+
+__device__ __forceinline__ RayState load_ray(const igxrt_ray* __restrict__ rays, uint32_t i,
+                                             uint32_t prev) {
+    const float4* p = reinterpret_cast<const float4*>(rays) + 2 * (size_t)i;
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    RayState r;
+    r.ox = a.x;
+    r.oy = a.y;
+    r.oz = a.z;
+    r.dx = b.x;
+    r.dy = b.y;
+    r.dz = b.z;
+    r.ix = __frcp_rn(safe_dir(b.x));
+    r.iy = __frcp_rn(safe_dir(b.y));
+    r.iz = __frcp_rn(safe_dir(b.z));
+    r.oix = __fmul_rn(a.x, r.ix);
+    r.oiy = __fmul_rn(a.y, r.iy);
+    r.oiz = __fmul_rn(a.z, r.iz);
+    r.tmin = a.w;
+    r.tmin_box = (a.w > -INFINITY) ? __fmaf_rn(-fabsf(a.w), 0x1p-10f, a.w) : -INFINITY;
+    r.tmax_eff = b.w < IGXRT_NO_HIT ? b.w : IGXRT_NO_HIT;
+    r.prev = prev;
+    return r;
+}
+
+__device__ __forceinline__ bool box_hit(const RayState& r, float lox, float hix, float loy,
+                                        float hiy, float loz, float hiz, float tcull, float& tn) {
+    const float t0x = __fmaf_rn(lox, r.ix, -r.oix), t1x = __fmaf_rn(hix, r.ix, -r.oix);
+    const float t0y = __fmaf_rn(loy, r.iy, -r.oiy), t1y = __fmaf_rn(hiy, r.iy, -r.oiy);
+    const float t0z = __fmaf_rn(loz, r.iz, -r.oiz), t1z = __fmaf_rn(hiz, r.iz, -r.oiz);
+    const float tnear =
+        fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), r.tmin_box));
+    const float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tcull));
+    tn = tnear;
+    return tnear <= tfar;
+}
+
+// rayIntersectTri's arithmetic on a primitive record {p0,prim}{e1,end}{e2,pad}.
+// Returns false when the u/v tests reject; otherwise t, u, v are the
+// reference's values (t may still be rejected by the caller).
+__device__ __forceinline__ bool tri_test(const RayState& r, const float4& v0, const float4& v1,
+                                         const float4& v2, float& t, float& u, float& v) {
+    // h = cross(dir, e2)
+    const float hx = __fsub_rn(__fmul_rn(r.dy, v2.z), __fmul_rn(v2.y, r.dz));
+    const float hy = __fsub_rn(__fmul_rn(r.dz, v2.x), __fmul_rn(v2.z, r.dx));
+    const float hz = __fsub_rn(__fmul_rn(r.dx, v2.y), __fmul_rn(v2.x, r.dy));
+    // a = dot(e1, h); f = 1 / a
+    const float a = __fadd_rn(__fadd_rn(__fmul_rn(v1.x, hx), __fmul_rn(v1.y, hy)), __fmul_rn(v1.z, hz));
+    const float f = __frcp_rn(a);
+    // s = pos - p0; u = f * dot(s, h)
+    const float sx = __fsub_rn(r.ox, v0.x), sy = __fsub_rn(r.oy, v0.y), sz = __fsub_rn(r.oz, v0.z);
+    u = __fmul_rn(f, __fadd_rn(__fadd_rn(__fmul_rn(sx, hx), __fmul_rn(sy, hy)), __fmul_rn(sz, hz)));
+    if (u < 0.f || u > 1.f)
+        return false;
+    // q = cross(s, e1); v = f * dot(dir, q)
+    const float qx = __fsub_rn(__fmul_rn(sy, v1.z), __fmul_rn(v1.y, sz));
+    const float qy = __fsub_rn(__fmul_rn(sz, v1.x), __fmul_rn(v1.z, sx));
+    const float qz = __fsub_rn(__fmul_rn(sx, v1.y), __fmul_rn(v1.x, sy));
+    v = __fmul_rn(f, __fadd_rn(__fadd_rn(__fmul_rn(r.dx, qx), __fmul_rn(r.dy, qy)), __fmul_rn(r.dz, qz)));
+    if (v < 0.f || __fadd_rn(u, v) > 1.f)
+        return false;
+    // t = f * dot(e2, q)
+    t = __fmul_rn(f, __fadd_rn(__fadd_rn(__fmul_rn(v2.x, qx), __fmul_rn(v2.y, qy)), __fmul_rn(v2.z, qz)));
+    return true;
+}
+
+// Traversal stack: the first `sh_depth` entries live in shared memory
+// (strided by the block size so a warp's pushes hit 32 banks), the rest in a
+// per-thread local array.
+struct TraversalStack {
+    uint32_t* sh;  // this thread's column of the block's shared stack
+    uint32_t stride;
+    uint32_t sh_depth;
+    uint32_t sp;
+    int32_t spill[kStackCapacityDevice];
+
+    __device__ __forceinline__ void push(int32_t v) {
+        if (sp < sh_depth)
+            sh[sp * stride] = (uint32_t)v;
+        else
+            spill[sp - sh_depth] = v;
+        ++sp;
+    }
+    __device__ __forceinline__ int32_t pop() {
+        --sp;
+        return sp < sh_depth ? (int32_t)sh[sp * stride] : spill[sp - sh_depth];
+    }
+};
+
+// Closest-hit / any-hit leaf processing.  Returns true when an any-hit query
+// is decided (occluder found).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool process_leaf(const float4* __restrict__ prims, int32_t ref,
+                                             const RayState& r, BestHit& best, uint32_t& pf) {
+    uint32_t i = (uint32_t)~ref;
+    for (;;) {
+        const float4* p = prims + 3 * (size_t)i;
+        const float4 v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
+        if (COUNT)
+            ++pf;
+        float t, u, v;
+        if (tri_test(r, v0, v1, v2, t, u, v)) {
+            const uint32_t prim = __float_as_uint(v0.w);
+            if (!(t <= r.tmin) && prim != r.prev) {
+                if (ANY) {
+                    if (t < r.tmax_eff)
+                        return true;
+                } else if (t < best.t || (t == best.t && prim < best.prim)) {
+                    best.t = t;
+                    best.u = u;
+                    best.v = v;
+                    best.prim = prim;
+                    best.tcull = cull_limit(t);
+                }
+            }
+        }
+        if (__float_as_uint(v1.w))
+            break;
+        ++i;
+    }
+    return false;
+}
+
+// Returns false if the stack would overflow (malformed BVH); `occluded` is
+// set for any-hit queries.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool traverse_bvh2(const float4* __restrict__ nodes,
+                                              const float4* __restrict__ prims,
+                                              const RayState& r, BestHit& best,
+                                              TraversalStack& st, bool& occluded, uint32_t& nf,
+                                              uint32_t& pf) {
+    int32_t next = 0;
+    for (;;) {
+        if (next >= 0) {
+            const float4* n = nodes + 4 * (size_t)next;
+            const float4 xy0 = __ldg(n), xy1 = __ldg(n + 1), z01 = __ldg(n + 2);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
+            if (COUNT)
+                ++nf;
+            float tn0, tn1;
+            const bool h0 = box_hit(r, xy0.x, xy0.y, xy0.z, xy0.w, z01.x, z01.y, best.tcull, tn0);
+            const bool h1 = box_hit(r, xy1.x, xy1.y, xy1.z, xy1.w, z01.z, z01.w, best.tcull, tn1);
+            if (h0 && h1) {
+                const bool first1 = tn1 < tn0;
+                if (st.sp >= kStackCapacityDevice)
+                    return false;
+                st.push(first1 ? ch.x : ch.y);
+                next = first1 ? ch.y : ch.x;
+            } else if (h0) {
+                next = ch.x;
+            } else if (h1) {
+                next = ch.y;
+            } else {
+                if (st.sp == 0)
+                    break;
+                next = st.pop();
+            }
+        } else {
+            if (process_leaf<ANY, COUNT>(prims, next, r, best, pf)) {
+                occluded = true;
+                return true;
+            }
+            if (st.sp == 0)
+                break;
+            next = st.pop();
+        }
+    }
+    return true;
+}
+
+struct SlotKey {
+    float tn;
+    int32_t child;
+    uint32_t slot;
+};
+
+__device__ __forceinline__ void order2(SlotKey& a, SlotKey& b) {
+    const bool swap = b.tn < a.tn || (b.tn == a.tn && b.slot < a.slot);
+    if (swap) {
+        const SlotKey t = a;
+        a = b;
+        b = t;
+    }
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool traverse_bvh4(const float4* __restrict__ nodes,
+                                              const float4* __restrict__ prims,
+                                              const RayState& r, BestHit& best,
+                                              TraversalStack& st, bool& occluded, uint32_t& nf,
+                                              uint32_t& pf) {
+    int32_t next = 0;
+    for (;;) {
+        if (next >= 0) {
+            const float4* n = nodes + 8 * (size_t)next;
+            const float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
+            const float4 lz = __ldg(n + 4), hz = __ldg(n + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(n + 6));
+            if (COUNT)
+                ++nf;
+            SlotKey k0, k1, k2, k3;
+            uint32_t m = 0;
+            float tn;
+            uint32_t h = box_hit(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, best.tcull, tn);
+            m += h;
+            k0 = {h ? tn : INFINITY, ch.x, 0u};
+            h = box_hit(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, best.tcull, tn);
+            m += h;
+            k1 = {h ? tn : INFINITY, ch.y, 1u};
+            h = box_hit(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, best.tcull, tn);
+            m += h;
+            k2 = {h ? tn : INFINITY, ch.z, 2u};
+            h = box_hit(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, best.tcull, tn);
+            m += h;
+            k3 = {h ? tn : INFINITY, ch.w, 3u};
+            if (m == 0) {
+                if (st.sp == 0)
+                    break;
+                next = st.pop();
+                continue;
+            }
+            // Sort (tnear, slot) ascending; missed slots carry +inf and sort
+            // last (a hit's tnear is at most the finite cull limit).
+            order2(k0, k1);
+            order2(k2, k3);
+            order2(k0, k2);
+            order2(k1, k3);
+            order2(k1, k2);
+            if (st.sp + m - 1 > kStackCapacityDevice)
+                return false;
+            if (m > 3)
+                st.push(k3.child);
+            if (m > 2)
+                st.push(k2.child);
+            if (m > 1)
+                st.push(k1.child);
+            next = k0.child;
+        } else {
+            if (process_leaf<ANY, COUNT>(prims, next, r, best, pf)) {
+                occluded = true;
+                return true;
+            }
+            if (st.sp == 0)
+                break;
+            next = st.pop();
+        }
+    }
+    return true;
+}
+
+}  // namespace igxrt

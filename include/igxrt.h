@@ -1,0 +1,288 @@
+/*
+ * igxrt.h — C ABI of the GB300 ray-query engine.
+ *
+ * This boundary replaces the compute dispatches through which igx_raytracing
+ * runs its ray queries:
+ *
+ *   - RaygenTask::prepareCommandList  (src/rt/task/raygen_task.cpp:88-94)
+ *       BindDescriptors + BindPipeline + Dispatch(W,H) of res/shaders/raygen.comp,
+ *       whose per-thread body is traceGeometry (res/shaders/trace.glsl:9-66);
+ *   - ShadowTask::prepareCommandList  (src/rt/task/shadow_task.cpp:194-213)
+ *       Dispatch(W,H,samples) of res/shaders/nv_all.shadow.comp, whose
+ *       per-thread body is traceOcclusion (res/shaders/trace.glsl:70-98);
+ *   - the scene buffers bound by SceneGraph::getDescriptors()
+ *       (res/shaders/scene.glsl:22-52; the SceneGraph class lives in the igx
+ *       submodule, which the reference checkout leaves empty).
+ *
+ * The reference loops linearly over every primitive; this engine builds a BVH
+ * on the host and traverses it with CUDA kernels for sm_103a.  The result of
+ * every query equals the linear loop's: the closest hit is the smallest t
+ * accepted by the reference's triangle test (res/shaders/primitive.glsl:239-284),
+ * ties going to the lowest primitive index (the loop runs in index order and
+ * accepts only t < hit.hitT).
+ *
+ * Conventions
+ *   - Every call returns igxrt_status; nothing throws across the ABI.
+ *   - igxrt_last_error(ctx) holds a message for the last failing call on ctx.
+ *   - The caller owns all arrays it passes.  The library owns device memory of
+ *     scenes and BVHs and the staging buffers of host-memory traces.
+ *   - Trace calls are ordered on the CUDA stream passed as `stream`
+ *     (a cudaStream_t cast to void*; NULL = the legacy default stream).
+ *     Without IGXRT_TRACE_HOST_MEMORY they return as soon as the work is queued.
+ *   - A context is used by one host thread at a time.  Scenes are immutable
+ *     after creation and may be traced from any context on the same device.
+ */
+#ifndef IGXRT_H
+#define IGXRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IGXRT_ABI_VERSION 1u
+
+/* res/shaders/primitive.glsl:6-7: the miss distance and the "no object" id. */
+#define IGXRT_NO_HIT 3.4028235e38f
+#define IGXRT_NO_RAY_HIT 0xFFFFFFFFu
+
+typedef enum igxrt_status {
+    IGXRT_OK = 0,
+    IGXRT_ERROR_INVALID_ARGUMENT = 1,
+    IGXRT_ERROR_CUDA = 2,
+    IGXRT_ERROR_OUT_OF_MEMORY = 3,
+    IGXRT_ERROR_INVALID_BVH = 4,
+    IGXRT_ERROR_KERNEL_STATUS = 5,  /* a kernel raised its error word */
+    IGXRT_ERROR_ADMISSION = 6,      /* request can never fit the memory cap */
+    IGXRT_ERROR_TIMEOUT = 7,
+    IGXRT_ERROR_UNSUPPORTED = 8,
+    IGXRT_ERROR_NOT_READY = 9,
+    IGXRT_ERROR_IO = 10
+} igxrt_status;
+
+/*
+ * Triangle record, 48 bytes: the std430 layout of GLSL `struct Triangle`
+ * (res/shaders/primitive.glsl:28-38).  n0..n2 are per-vertex normals packed
+ * as two halves (decoded by decodeSpheremap, primitive.glsl:95-104); the
+ * traversal ignores them.
+ */
+typedef struct igxrt_triangle {
+    float p0[3];
+    uint32_t n0;
+    float p1[3];
+    uint32_t n1;
+    float p2[3];
+    uint32_t n2;
+} igxrt_triangle;
+
+/*
+ * Ray, 32 bytes: the std430 layout of GLSL `struct Ray { vec3 pos; vec3 dir; }`
+ * (primitive.glsl:23-26) with the two padding words used for the interval.
+ * A triangle is accepted when t > tmin (the reference rejects t <= 0,
+ * primitive.glsl:276, so tmin = 0 reproduces it) and t < min(tmax, IGXRT_NO_HIT)
+ * (the reference starts hit.hitT at noHit, trace.glsl:14; for the any-hit
+ * query tmax is traceOcclusion's maxDist, trace.glsl:70,97).
+ * The direction need not be normalised; t is in units of |dir|.
+ */
+typedef struct igxrt_ray {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} igxrt_ray;
+
+/*
+ * Closest-hit record, 16 bytes: the fields of GLSL `struct Hit`
+ * (primitive.glsl:9-21) that the traversal decides: hitT, uv and object.
+ * A miss is {IGXRT_NO_HIT, 0, 0, IGXRT_NO_RAY_HIT}.
+ */
+typedef struct igxrt_hit {
+    float t;
+    float u;
+    float v;
+    uint32_t prim;
+} igxrt_hit;
+
+/* ---- BVH layouts (device and export format) ---------------------------- */
+
+/* Node layouts the builder can emit. */
+#define IGXRT_LAYOUT_BVH2 0u /* binary, 64-byte nodes holding both child boxes */
+#define IGXRT_LAYOUT_BVH4 1u /* 4-wide, 128-byte nodes holding four child boxes */
+#define IGXRT_LAYOUT_COUNT 2u
+
+/*
+ * BVH2 node, 64 bytes, 64-byte aligned; read as four 128-bit loads.
+ * Child c's box is [x[c][0],x[c][1]] x [y[c][0],y[c][1]] x [z[c][0],z[c][1]],
+ * already widened outward by the builder's padding.  child[c] >= 0 is the
+ * index of an interior node; child[c] < 0 is a leaf whose first primitive
+ * record is ~child[c]; the leaf runs to the record flagged leaf_end.
+ * An absent child has the box {+inf,+inf} on every axis, which no ray enters.
+ */
+typedef struct igxrt_bvh2_node {
+    float c0_x[2], c0_y[2];
+    float c1_x[2], c1_y[2];
+    float c0_z[2], c1_z[2];
+    int32_t child[2];
+    uint32_t pad[2];
+} igxrt_bvh2_node;
+
+/*
+ * BVH4 node, 128 bytes, 128-byte aligned; read as eight 128-bit loads.
+ * Per axis a, lo[a][i] / hi[a][i] is child i's slab.  child[i] as in BVH2;
+ * unused slots carry the {+inf,+inf} box.
+ */
+typedef struct igxrt_bvh4_node {
+    float lo_x[4], hi_x[4];
+    float lo_y[4], hi_y[4];
+    float lo_z[4], hi_z[4];
+    int32_t child[4];
+    uint32_t pad[4];
+} igxrt_bvh4_node;
+
+/*
+ * Primitive record, 48 bytes, in leaf order.  e1 = p1 - p0 and e2 = p2 - p0
+ * are the same binary32 subtractions rayIntersectTri performs
+ * (primitive.glsl:245-246), stored so the kernel does not repeat them.
+ */
+typedef struct igxrt_prim_record {
+    float p0[3];
+    uint32_t prim;     /* index of the triangle in the caller's array */
+    float e1[3];
+    uint32_t leaf_end; /* 1 on the last record of a leaf, else 0 */
+    float e2[3];
+    uint32_t pad;
+} igxrt_prim_record;
+
+typedef struct igxrt_build_options {
+    uint32_t max_leaf_size; /* 0 = 8; at most 16 */
+    uint32_t sah_bins;      /* 0 = 32 */
+    float node_cost;        /* SAH cost of a node visit, 0 = 1.0 */
+    float tri_cost;         /* SAH cost of a triangle test, 0 = 1.0 */
+    uint32_t threads;       /* host build threads, 0 = all cores */
+    uint32_t reserved[3];
+} igxrt_build_options;
+
+typedef struct igxrt_bvh_info {
+    uint32_t triangle_count;
+    uint32_t bvh2_nodes;
+    uint32_t bvh4_nodes;
+    uint32_t leaf_count;
+    uint32_t max_depth;
+    uint32_t max_leaf_size;
+    float sah_cost;
+    float bounds[6]; /* min xyz, max xyz of the triangles */
+    float pad_abs;   /* absolute outward padding added to every node box */
+    uint32_t max_stack[IGXRT_LAYOUT_COUNT]; /* deepest traversal stack per layout */
+    uint64_t device_bytes;
+} igxrt_bvh_info;
+
+typedef struct igxrt_bvh igxrt_bvh;
+typedef struct igxrt_context igxrt_context;
+typedef struct igxrt_scene igxrt_scene;
+
+/* ---- Host-side BVH (no GPU needed) --------------------------------------- */
+
+/* Builds a binned-SAH BVH over `count` triangles on the host (count may be 0).
+ * Rejects non-finite vertex coordinates with IGXRT_ERROR_INVALID_ARGUMENT. */
+igxrt_status igxrt_bvh_build(const igxrt_triangle* tris, uint32_t count,
+                             const igxrt_build_options* opts, igxrt_bvh** out);
+igxrt_status igxrt_bvh_destroy(igxrt_bvh* bvh);
+igxrt_status igxrt_bvh_get_info(const igxrt_bvh* bvh, igxrt_bvh_info* info);
+/* Borrowed pointers to the node array of `layout` and the primitive records;
+ * valid until igxrt_bvh_destroy. */
+igxrt_status igxrt_bvh_get_data(const igxrt_bvh* bvh, uint32_t layout,
+                                const void** nodes, uint64_t* node_count,
+                                const igxrt_prim_record** prims, uint64_t* prim_count);
+/* Checks structure and boxes: every triangle in exactly one leaf, every child
+ * box contains its subtree, node indices in range, depth within the limit. */
+igxrt_status igxrt_bvh_validate(const igxrt_bvh* bvh, char* msg, size_t msg_len);
+/* Serialises a built BVH (both layouts and the triangle array) to a file and
+ * loads it back, so a server can warm-start without rebuilding. */
+igxrt_status igxrt_bvh_save(const igxrt_bvh* bvh, const char* path);
+igxrt_status igxrt_bvh_load(const char* path, igxrt_bvh** out);
+
+/* ---- Context and resident scenes ---------------------------------------- */
+
+igxrt_status igxrt_create(int device, igxrt_context** out);
+igxrt_status igxrt_destroy(igxrt_context* ctx);
+const char* igxrt_last_error(const igxrt_context* ctx);
+/* Static description of a status code. */
+const char* igxrt_status_string(igxrt_status status);
+
+/* Builds the BVH on the host and uploads nodes, primitive records and the
+ * triangle array to the context's device. */
+igxrt_status igxrt_scene_create(igxrt_context* ctx, const igxrt_triangle* tris,
+                                uint32_t count, const igxrt_build_options* opts,
+                                igxrt_scene** out);
+/* Uploads an already built BVH. */
+igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bvh,
+                                         igxrt_scene** out);
+igxrt_status igxrt_scene_destroy(igxrt_scene* scene);
+igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info);
+
+/* ---- Ray queries --------------------------------------------------------- */
+
+/* rays, prev_hit and the output are host pointers: the call stages them
+ * through device buffers and returns once the results are in host memory. */
+#define IGXRT_TRACE_HOST_MEMORY 1u
+
+/* Launch shape of the traversal kernels. Zero fields take the defaults. */
+typedef struct igxrt_launch_params {
+    uint32_t block_size;  /* threads per CTA: 64, 128 or 256 */
+    uint32_t stack_depth; /* shared-memory stack entries per thread: 8, 16 or 32;
+                             deeper entries spill to local memory */
+    uint32_t packet_size; /* rays taken per queue fetch: 32, 64 or 128 */
+    uint32_t layout;      /* IGXRT_LAYOUT_* */
+    uint32_t ctas_per_sm; /* persistent CTAs per SM, 0 = as many as fit */
+    uint32_t reserved[3];
+} igxrt_launch_params;
+
+igxrt_status igxrt_set_launch_params(igxrt_context* ctx, const igxrt_launch_params* p);
+igxrt_status igxrt_get_launch_params(const igxrt_context* ctx, igxrt_launch_params* p);
+
+/*
+ * Closest hit (traceGeometry, trace.glsl:9-66) for `count` rays.
+ * prev_hit may be NULL; otherwise prev_hit[i] is a triangle index that ray i
+ * must not hit (the reference's prevHit; IGXRT_NO_RAY_HIT excludes nothing).
+ */
+igxrt_status igxrt_trace_closest(igxrt_context* ctx, const igxrt_scene* scene,
+                                 const igxrt_ray* rays, const uint32_t* prev_hit,
+                                 uint32_t count, igxrt_hit* hits, uint32_t flags,
+                                 void* stream);
+
+/*
+ * Occlusion (traceOcclusion, trace.glsl:70-98): occluded[i] = 1 when some
+ * triangle other than prev_hit[i] is accepted with tmin < t < tmax, else 0.
+ * The kernel stops at the first such triangle.
+ */
+igxrt_status igxrt_trace_any(igxrt_context* ctx, const igxrt_scene* scene,
+                             const igxrt_ray* rays, const uint32_t* prev_hit,
+                             uint32_t count, uint32_t* occluded, uint32_t flags,
+                             void* stream);
+
+/* Copies `count` device hits to host memory and waits for them. */
+igxrt_status igxrt_fetch_hits(igxrt_context* ctx, const igxrt_hit* device_hits,
+                              uint32_t count, igxrt_hit* host_hits, void* stream);
+
+/* Waits for the stream and reports a kernel error word raised since the last
+ * call (IGXRT_ERROR_KERNEL_STATUS). */
+igxrt_status igxrt_sync(igxrt_context* ctx, void* stream);
+
+/*
+ * Instrumented traversal: per ray, the number of node records and primitive
+ * records the closest (mode 0) or any-hit (mode 1) kernel fetches.  Used for
+ * the bytes-per-ray roofline; the traversal order is the production kernel's.
+ */
+igxrt_status igxrt_count_fetches(igxrt_context* ctx, const igxrt_scene* scene,
+                                 const igxrt_ray* rays, const uint32_t* prev_hit,
+                                 uint32_t count, uint32_t mode, uint32_t layout,
+                                 uint32_t* node_fetches, uint32_t* prim_fetches,
+                                 void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IGXRT_H */

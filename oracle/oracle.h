@@ -1,0 +1,72 @@
+/*
+ * oracle.h — CPU restatement of igx_raytracing's ray-query path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
+ * engine and the timed CPU baseline; the engine never links, loads or calls
+ * it.  Only the test suite, the smoke check and the benchmark's CPU-baseline
+ * leg use it.
+ *
+ * Two parts:
+ *  - orc_trace_geometry / orc_trace_occlusion: brute-force loops over every
+ *    triangle in index order, restating traceGeometry / traceOcclusion
+ *    (res/shaders/trace.glsl:9-66, 70-98) around rayIntersectTri
+ *    (res/shaders/primitive.glsl:239-284) in IEEE binary32 with no FMA
+ *    contraction.  These define the expected results.
+ *  - orc_bvh_trace: the same triangle test driven by a traversal of the
+ *    engine's exported BVH (the layouts in include/igxrt.h), visiting nodes in
+ *    the order the CUDA kernels do.  It is the multi-threaded CPU baseline and
+ *    counts node and primitive records fetched per ray (the roofline's bytes).
+ */
+#ifndef IGXRT_ORACLE_H
+#define IGXRT_ORACLE_H
+
+#include <stdint.h>
+#include "igxrt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-ray event flags reported by the brute-force loops. */
+#define ORC_EVENT_NAN_T 1u    /* a NaN t was accepted: the linear loop's later
+                                 decisions then depend on index order alone */
+#define ORC_EVENT_ZERO_DET 2u /* a == 0 for a triangle whose u, v tests passed */
+
+/* Brute-force closest hit.  flags may be NULL.  threads <= 0: all cores. */
+void orc_trace_geometry(const igxrt_triangle* tris, uint32_t ntri,
+                        const igxrt_ray* rays, const uint32_t* prev_hit,
+                        uint32_t nrays, igxrt_hit* out, uint32_t* flags,
+                        int threads);
+
+/* Brute-force occlusion: out[i] = traceOcclusion(ray, rays[i].tmax, prev). */
+void orc_trace_occlusion(const igxrt_triangle* tris, uint32_t ntri,
+                         const igxrt_ray* rays, const uint32_t* prev_hit,
+                         uint32_t nrays, uint32_t* out, uint32_t* flags,
+                         int threads);
+
+/* Closest hit of one ray against one triangle in binary64, for logging
+ * disagreements: returns 1 and fills t,u,v if the exact-arithmetic-style
+ * test (same formulas, double precision) accepts. */
+int orc_reintersect_f64(const igxrt_ray* ray, const igxrt_triangle* tri,
+                        double* t, double* u, double* v);
+
+/*
+ * BVH traversal on the CPU.  layout = IGXRT_LAYOUT_BVH2 or _BVH4; nodes and
+ * prims as returned by igxrt_bvh_get_data.  mode 0 = closest (out_hits),
+ * mode 1 = any (out_occluded).  node_fetches / prim_fetches may be NULL.
+ * Returns 0, or -1 on a malformed BVH (stack overflow / bad index).
+ */
+int orc_bvh_trace(uint32_t layout, const void* nodes, uint64_t node_count,
+                  const igxrt_prim_record* prims, uint64_t prim_count,
+                  const igxrt_ray* rays, const uint32_t* prev_hit, uint32_t nrays,
+                  uint32_t mode, igxrt_hit* out_hits, uint32_t* out_occluded,
+                  uint32_t* node_fetches, uint32_t* prim_fetches, int threads);
+
+/* Number of hardware threads the oracle uses for threads <= 0. */
+int orc_hardware_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,600 @@
+/*
+ * trace_oracle.c — CPU restatement of igx_raytracing's ray-query path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA engine and the timed
+ * CPU baseline.  The engine never links or calls this file.
+ *
+ * Arithmetic contract (the same one the CUDA kernels follow):
+ *   - IEEE binary32, round to nearest, denormals kept (no flush to zero);
+ *   - compiled with -ffp-contract=off: no multiply-add fusion anywhere in the
+ *     triangle test;
+ *   - GLSL dot(a,b) = a.x*b.x + a.y*b.y + a.z*b.z summed left to right;
+ *   - GLSL cross(a,b) = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y);
+ *   - 1/a is a correctly rounded division.
+ * The BVH box test uses explicit fmaf(), which is correctly rounded on the
+ * host and on the GPU alike, so both make identical culling decisions.
+ */
+#define _GNU_SOURCE
+#include "oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+typedef struct {
+    float x, y, z;
+} v3;
+
+static inline v3 mk(const float* p) {
+    v3 r = {p[0], p[1], p[2]};
+    return r;
+}
+static inline v3 sub(v3 a, v3 b) {
+    v3 r = {a.x - b.x, a.y - b.y, a.z - b.z};
+    return r;
+}
+/* GLSL cross() component order. */
+static inline v3 cross(v3 a, v3 b) {
+    v3 r = {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+    return r;
+}
+/* GLSL dot(), summed left to right. */
+static inline float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+static inline float tmax_effective(float tmax) {
+    /* The reference starts hit.hitT at noHit (trace.glsl:14, 73); a larger
+     * or NaN tmax therefore behaves as noHit. */
+    return tmax < IGXRT_NO_HIT ? tmax : IGXRT_NO_HIT;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Brute force: traceGeometry / traceOcclusion around rayIntersectTri.      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    float hitT;
+    float u, v;
+    uint32_t object;
+    uint32_t events;
+} hitstate;
+
+/*
+ * rayIntersectTri, res/shaders/primitive.glsl:239-284, step for step.
+ * `tmin` generalises the reference's `t <= 0` rejection (tmin = 0 there).
+ */
+static int ray_intersect_tri(v3 pos, v3 dir, float tmin, const igxrt_triangle* tri,
+                             uint64_t obj, uint64_t prevObj, hitstate* hit) {
+    const v3 p0 = mk(tri->p0);
+    const v3 p1 = mk(tri->p1);
+    const v3 p2 = mk(tri->p2);
+
+    const v3 p1_p0 = sub(p1, p0); /* :245 */
+    const v3 p2_p0 = sub(p2, p0); /* :246 */
+
+    const v3 h = cross(dir, p2_p0); /* :255 */
+    const float a = dot(p1_p0, h);  /* :256 */
+
+    if (fabsf(a) < 0) /* :258, never true: kept as written */
+        return 0;
+
+    const float f = 1 / a;          /* :261 */
+    const v3 s = sub(pos, p0);      /* :262 */
+    const float u = f * dot(s, h);  /* :263 */
+
+    if (u < 0 || u > 1) /* :265 */
+        return 0;
+
+    const v3 q = cross(s, p1_p0);     /* :268 */
+    const float v = f * dot(dir, q);  /* :269 */
+
+    if (v < 0 || u + v > 1) /* :271 */
+        return 0;
+
+    if (a == 0)
+        hit->events |= ORC_EVENT_ZERO_DET;
+
+    const float t = f * dot(p2_p0, q); /* :274 */
+
+    if (t <= tmin || obj == prevObj || t >= hit->hitT) /* :276 */
+        return 0;
+
+    if (t != t)
+        hit->events |= ORC_EVENT_NAN_T;
+
+    hit->u = u; /* :279-280 */
+    hit->v = v;
+    hit->hitT = t;
+    return 1;
+}
+
+/* traceGeometry, res/shaders/trace.glsl:9-66 (triangle loop :24-28). */
+static void trace_geometry_one(const igxrt_triangle* tris, uint32_t ntri,
+                               const igxrt_ray* ray, uint32_t prev, igxrt_hit* out,
+                               uint32_t* flags) {
+    hitstate hit;
+    hit.hitT = tmax_effective(ray->tmax); /* :14 (noHit at the default tmax) */
+    hit.u = hit.v = 0;                    /* :16 */
+    hit.object = 0;                       /* :17 */
+    hit.events = 0;
+    const v3 pos = mk(ray->org), dir = mk(ray->dir);
+    int found = 0;
+    uint32_t j = 0;
+    for (uint32_t i = 0; i < ntri; ++i, ++j)
+        if (ray_intersect_tri(pos, dir, ray->tmin, &tris[i], j, (uint64_t)prev, &hit)) {
+            hit.object = j; /* :27 */
+            found = 1;
+        }
+    if (found) {
+        out->t = hit.hitT;
+        out->u = hit.u;
+        out->v = hit.v;
+        out->prim = hit.object;
+    } else {
+        /* raygen.comp:40-41 encodes a miss as object = noRayHit. */
+        out->t = IGXRT_NO_HIT;
+        out->u = 0;
+        out->v = 0;
+        out->prim = IGXRT_NO_RAY_HIT;
+    }
+    if (flags)
+        *flags = hit.events;
+}
+
+/* traceOcclusion, res/shaders/trace.glsl:70-98. */
+static void trace_occlusion_one(const igxrt_triangle* tris, uint32_t ntri,
+                                const igxrt_ray* ray, uint32_t prev, uint32_t* out,
+                                uint32_t* flags) {
+    hitstate hit;
+    hit.hitT = IGXRT_NO_HIT; /* :73 */
+    hit.u = hit.v = 0;
+    hit.object = 0;
+    hit.events = 0;
+    const v3 pos = mk(ray->org), dir = mk(ray->dir);
+    uint32_t j = 0;
+    for (uint32_t i = 0; i < ntri; ++i, ++j) /* :77-79 */
+        ray_intersect_tri(pos, dir, ray->tmin, &tris[i], j, (uint64_t)prev, &hit);
+    const float maxDist = tmax_effective(ray->tmax);
+    *out = hit.hitT < maxDist ? 1u : 0u; /* :97 */
+    if (flags)
+        *flags = hit.events;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Thread pool over ray chunks.                                             */
+/* ------------------------------------------------------------------------ */
+
+typedef void (*chunk_fn)(void* ctx, uint32_t begin, uint32_t end);
+
+typedef struct {
+    chunk_fn fn;
+    void* ctx;
+    uint32_t n;
+    uint32_t chunk;
+    _Atomic uint32_t next;
+} pool_job;
+
+static void* pool_worker(void* arg) {
+    pool_job* job = (pool_job*)arg;
+    for (;;) {
+        uint32_t b = atomic_fetch_add(&job->next, job->chunk);
+        if (b >= job->n)
+            break;
+        uint32_t e = b + job->chunk;
+        if (e > job->n || e < b)
+            e = job->n;
+        job->fn(job->ctx, b, e);
+    }
+    return NULL;
+}
+
+int orc_hardware_threads(void) {
+    long n = sysconf(_SC_NPROCESSORS_ONLN);
+    return n > 0 ? (int)n : 1;
+}
+
+static void run_parallel(chunk_fn fn, void* ctx, uint32_t n, uint32_t chunk, int threads) {
+    if (threads <= 0)
+        threads = orc_hardware_threads();
+    if (n == 0)
+        return;
+    pool_job job;
+    job.fn = fn;
+    job.ctx = ctx;
+    job.n = n;
+    job.chunk = chunk;
+    atomic_init(&job.next, 0);
+    if (threads == 1) {
+        pool_worker(&job);
+        return;
+    }
+    pthread_t* tid = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+    int started = 0;
+    for (int i = 0; i < threads; ++i)
+        if (pthread_create(&tid[i], NULL, pool_worker, &job) == 0)
+            ++started;
+    if (started == 0)
+        pool_worker(&job);
+    for (int i = 0; i < started; ++i)
+        pthread_join(tid[i], NULL);
+    free(tid);
+}
+
+typedef struct {
+    const igxrt_triangle* tris;
+    uint32_t ntri;
+    const igxrt_ray* rays;
+    const uint32_t* prev;
+    igxrt_hit* hits;
+    uint32_t* occ;
+    uint32_t* flags;
+} brute_ctx;
+
+static void brute_closest_chunk(void* p, uint32_t b, uint32_t e) {
+    brute_ctx* c = (brute_ctx*)p;
+    for (uint32_t i = b; i < e; ++i)
+        trace_geometry_one(c->tris, c->ntri, &c->rays[i],
+                           c->prev ? c->prev[i] : IGXRT_NO_RAY_HIT, &c->hits[i],
+                           c->flags ? &c->flags[i] : NULL);
+}
+
+static void brute_any_chunk(void* p, uint32_t b, uint32_t e) {
+    brute_ctx* c = (brute_ctx*)p;
+    for (uint32_t i = b; i < e; ++i)
+        trace_occlusion_one(c->tris, c->ntri, &c->rays[i],
+                            c->prev ? c->prev[i] : IGXRT_NO_RAY_HIT, &c->occ[i],
+                            c->flags ? &c->flags[i] : NULL);
+}
+
+void orc_trace_geometry(const igxrt_triangle* tris, uint32_t ntri, const igxrt_ray* rays,
+                        const uint32_t* prev_hit, uint32_t nrays, igxrt_hit* out,
+                        uint32_t* flags, int threads) {
+    brute_ctx c = {tris, ntri, rays, prev_hit, out, NULL, flags};
+    run_parallel(brute_closest_chunk, &c, nrays, 64, threads);
+}
+
+void orc_trace_occlusion(const igxrt_triangle* tris, uint32_t ntri, const igxrt_ray* rays,
+                         const uint32_t* prev_hit, uint32_t nrays, uint32_t* out,
+                         uint32_t* flags, int threads) {
+    brute_ctx c = {tris, ntri, rays, prev_hit, NULL, out, flags};
+    run_parallel(brute_any_chunk, &c, nrays, 64, threads);
+}
+
+int orc_reintersect_f64(const igxrt_ray* ray, const igxrt_triangle* tri, double* t_out,
+                        double* u_out, double* v_out) {
+    double o[3], d[3], p0[3], e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+        o[k] = ray->org[k];
+        d[k] = ray->dir[k];
+        p0[k] = tri->p0[k];
+        e1[k] = (double)tri->p1[k] - (double)tri->p0[k];
+        e2[k] = (double)tri->p2[k] - (double)tri->p0[k];
+    }
+    double h[3] = {d[1] * e2[2] - e2[1] * d[2], d[2] * e2[0] - e2[2] * d[0],
+                   d[0] * e2[1] - e2[0] * d[1]};
+    double a = e1[0] * h[0] + e1[1] * h[1] + e1[2] * h[2];
+    double s[3] = {o[0] - p0[0], o[1] - p0[1], o[2] - p0[2]};
+    double q[3] = {s[1] * e1[2] - e1[1] * s[2], s[2] * e1[0] - e1[2] * s[0],
+                   s[0] * e1[1] - e1[0] * s[1]};
+    double u = (s[0] * h[0] + s[1] * h[1] + s[2] * h[2]) / a;
+    double v = (d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) / a;
+    double t = (e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) / a;
+    *t_out = t;
+    *u_out = u;
+    *v_out = v;
+    return (u >= 0 && u <= 1 && v >= 0 && u + v <= 1 && t > (double)ray->tmin) ? 1 : 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* BVH traversal (the CPU baseline and fetch counter).                      */
+/* ------------------------------------------------------------------------ */
+
+#define ORC_STACK 256
+
+typedef struct {
+    v3 o, d;     /* the ray as given: the triangle test uses these */
+    v3 idir;     /* 1/d, with |d| < 2^-80 raised to 2^-80 keeping the sign */
+    v3 ood;      /* o * idir */
+    float tmin;
+    float tmin_box;
+    float tmax_eff;
+    uint32_t prev;
+} rayprep;
+
+static inline float safe_dir(float d) {
+    return fabsf(d) < 0x1p-80f ? copysignf(0x1p-80f, d) : d;
+}
+
+static void prep_ray(const igxrt_ray* r, uint32_t prev, rayprep* p) {
+    p->o = mk(r->org);
+    p->d = mk(r->dir);
+    p->idir.x = 1.0f / safe_dir(r->dir[0]);
+    p->idir.y = 1.0f / safe_dir(r->dir[1]);
+    p->idir.z = 1.0f / safe_dir(r->dir[2]);
+    p->ood.x = p->o.x * p->idir.x;
+    p->ood.y = p->o.y * p->idir.y;
+    p->ood.z = p->o.z * p->idir.z;
+    p->tmin = r->tmin;
+    p->tmin_box = (r->tmin > -INFINITY) ? fmaf(-fabsf(r->tmin), 0x1p-10f, r->tmin) : -INFINITY;
+    p->tmax_eff = tmax_effective(r->tmax);
+    p->prev = prev;
+}
+
+/* Slab test against a padded box; identical operation sequence on the GPU. */
+static inline int box_hit(const rayprep* r, float lox, float hix, float loy, float hiy,
+                          float loz, float hiz, float tcull, float* tnear) {
+    const float t0x = fmaf(lox, r->idir.x, -r->ood.x), t1x = fmaf(hix, r->idir.x, -r->ood.x);
+    const float t0y = fmaf(loy, r->idir.y, -r->ood.y), t1y = fmaf(hiy, r->idir.y, -r->ood.y);
+    const float t0z = fmaf(loz, r->idir.z, -r->ood.z), t1z = fmaf(hiz, r->idir.z, -r->ood.z);
+    const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)),
+                           fmaxf(fminf(t0z, t1z), r->tmin_box));
+    const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)),
+                           fminf(fmaxf(t0z, t1z), tcull));
+    *tnear = tn;
+    return tn <= tf;
+}
+
+/* rayIntersectTri's arithmetic on a primitive record (e1, e2 stored). */
+static inline int rec_intersect(const rayprep* r, const igxrt_prim_record* rec, float* t_out,
+                                float* u_out, float* v_out) {
+    const v3 p0 = mk(rec->p0), e1 = mk(rec->e1), e2 = mk(rec->e2);
+    const v3 h = cross(r->d, e2);
+    const float a = dot(e1, h);
+    const float f = 1 / a;
+    const v3 s = sub(r->o, p0);
+    const float u = f * dot(s, h);
+    if (u < 0 || u > 1)
+        return 0;
+    const v3 q = cross(s, e1);
+    const float v = f * dot(r->d, q);
+    if (v < 0 || u + v > 1)
+        return 0;
+    *t_out = f * dot(e2, q);
+    *u_out = u;
+    *v_out = v;
+    return 1;
+}
+
+typedef struct {
+    float t, u, v;
+    uint32_t prim;
+    float tcull;
+} best_hit;
+
+/* Box cull limit: best t widened by 2^-10, kept finite so the {+inf} box of
+ * an absent child is never entered. */
+static inline float cull_limit(float t) { return fminf(fmaf(t, 0x1p-10f, t), FLT_MAX); }
+
+/* Returns 1 when the record is accepted under the (t, prim) order. */
+static inline int leaf_record(const rayprep* r, const igxrt_prim_record* rec, best_hit* b,
+                              int anyhit) {
+    float t, u, v;
+    if (!rec_intersect(r, rec, &t, &u, &v))
+        return 0;
+    if (t <= r->tmin || rec->prim == r->prev)
+        return 0;
+    if (anyhit)
+        return t < r->tmax_eff;
+    if (t < b->t || (t == b->t && rec->prim < b->prim)) {
+        b->t = t;
+        b->u = u;
+        b->v = v;
+        b->prim = rec->prim;
+        b->tcull = cull_limit(t);
+        return 1;
+    }
+    return 0;
+}
+
+static int bvh2_trace_one(const igxrt_bvh2_node* nodes, uint64_t nn,
+                          const igxrt_prim_record* prims, uint64_t np, const rayprep* r,
+                          int anyhit, best_hit* b, uint32_t* occluded, uint32_t* nf,
+                          uint32_t* pf) {
+    int32_t stack[ORC_STACK];
+    int sp = 0;
+    *occluded = 0;
+    if (nn == 0)
+        return 0;
+    int32_t next = 0;
+    for (;;) {
+        if (next >= 0) {
+            if ((uint64_t)next >= nn)
+                return -1;
+            const igxrt_bvh2_node* n = &nodes[next];
+            ++*nf;
+            float tn0, tn1;
+            const int h0 = box_hit(r, n->c0_x[0], n->c0_x[1], n->c0_y[0], n->c0_y[1],
+                                   n->c0_z[0], n->c0_z[1], b->tcull, &tn0);
+            const int h1 = box_hit(r, n->c1_x[0], n->c1_x[1], n->c1_y[0], n->c1_y[1],
+                                   n->c1_z[0], n->c1_z[1], b->tcull, &tn1);
+            if (h0 && h1) {
+                const int first = tn1 < tn0 ? 1 : 0;
+                if (sp >= ORC_STACK)
+                    return -1;
+                stack[sp++] = n->child[1 - first];
+                next = n->child[first];
+            } else if (h0) {
+                next = n->child[0];
+            } else if (h1) {
+                next = n->child[1];
+            } else {
+                if (sp == 0)
+                    break;
+                next = stack[--sp];
+            }
+        } else {
+            uint64_t i = (uint64_t)(uint32_t)~next;
+            for (;;) {
+                if (i >= np)
+                    return -1;
+                const igxrt_prim_record* rec = &prims[i];
+                ++*pf;
+                if (leaf_record(r, rec, b, anyhit) && anyhit) {
+                    *occluded = 1;
+                    return 0;
+                }
+                if (rec->leaf_end)
+                    break;
+                ++i;
+            }
+            if (sp == 0)
+                break;
+            next = stack[--sp];
+        }
+    }
+    return 0;
+}
+
+static int bvh4_trace_one(const igxrt_bvh4_node* nodes, uint64_t nn,
+                          const igxrt_prim_record* prims, uint64_t np, const rayprep* r,
+                          int anyhit, best_hit* b, uint32_t* occluded, uint32_t* nf,
+                          uint32_t* pf) {
+    int32_t stack[ORC_STACK];
+    int sp = 0;
+    *occluded = 0;
+    if (nn == 0)
+        return 0;
+    int32_t next = 0;
+    for (;;) {
+        if (next >= 0) {
+            if ((uint64_t)next >= nn)
+                return -1;
+            const igxrt_bvh4_node* n = &nodes[next];
+            ++*nf;
+            float tn[4];
+            int slot[4];
+            int m = 0;
+            for (int k = 0; k < 4; ++k) {
+                float t;
+                if (box_hit(r, n->lo_x[k], n->hi_x[k], n->lo_y[k], n->hi_y[k], n->lo_z[k],
+                            n->hi_z[k], b->tcull, &t)) {
+                    /* insertion by (tnear, slot): stable for equal tnear */
+                    int j = m++;
+                    while (j > 0 && t < tn[j - 1]) {
+                        tn[j] = tn[j - 1];
+                        slot[j] = slot[j - 1];
+                        --j;
+                    }
+                    tn[j] = t;
+                    slot[j] = k;
+                }
+            }
+            if (m == 0) {
+                if (sp == 0)
+                    break;
+                next = stack[--sp];
+            } else {
+                if (sp + m - 1 > ORC_STACK)
+                    return -1;
+                for (int j = m - 1; j >= 1; --j)
+                    stack[sp++] = n->child[slot[j]];
+                next = n->child[slot[0]];
+            }
+        } else {
+            uint64_t i = (uint64_t)(uint32_t)~next;
+            for (;;) {
+                if (i >= np)
+                    return -1;
+                const igxrt_prim_record* rec = &prims[i];
+                ++*pf;
+                if (leaf_record(r, rec, b, anyhit) && anyhit) {
+                    *occluded = 1;
+                    return 0;
+                }
+                if (rec->leaf_end)
+                    break;
+                ++i;
+            }
+            if (sp == 0)
+                break;
+            next = stack[--sp];
+        }
+    }
+    return 0;
+}
+
+typedef struct {
+    uint32_t layout;
+    const void* nodes;
+    uint64_t nn;
+    const igxrt_prim_record* prims;
+    uint64_t np;
+    const igxrt_ray* rays;
+    const uint32_t* prev;
+    uint32_t mode;
+    igxrt_hit* hits;
+    uint32_t* occ;
+    uint32_t* nf;
+    uint32_t* pf;
+    _Atomic int error;
+} bvh_ctx;
+
+static void bvh_chunk(void* p, uint32_t b0, uint32_t e0) {
+    bvh_ctx* c = (bvh_ctx*)p;
+    for (uint32_t i = b0; i < e0; ++i) {
+        rayprep r;
+        prep_ray(&c->rays[i], c->prev ? c->prev[i] : IGXRT_NO_RAY_HIT, &r);
+        best_hit b;
+        b.t = r.tmax_eff;
+        b.u = 0;
+        b.v = 0;
+        b.prim = 0; /* "prim < b.prim" never holds until a first hit */
+        b.tcull = cull_limit(b.t);
+        uint32_t occ = 0, nf = 0, pf = 0;
+        int rc;
+        if (c->layout == IGXRT_LAYOUT_BVH4)
+            rc = bvh4_trace_one((const igxrt_bvh4_node*)c->nodes, c->nn, c->prims, c->np, &r,
+                                c->mode == 1, &b, &occ, &nf, &pf);
+        else
+            rc = bvh2_trace_one((const igxrt_bvh2_node*)c->nodes, c->nn, c->prims, c->np, &r,
+                                c->mode == 1, &b, &occ, &nf, &pf);
+        if (rc != 0)
+            atomic_store(&c->error, 1);
+        if (c->mode == 1) {
+            if (c->occ)
+                c->occ[i] = occ;
+        } else if (c->hits) {
+            if (b.t < r.tmax_eff) {
+                c->hits[i].t = b.t;
+                c->hits[i].u = b.u;
+                c->hits[i].v = b.v;
+                c->hits[i].prim = b.prim;
+            } else {
+                c->hits[i].t = IGXRT_NO_HIT;
+                c->hits[i].u = 0;
+                c->hits[i].v = 0;
+                c->hits[i].prim = IGXRT_NO_RAY_HIT;
+            }
+        }
+        if (c->nf)
+            c->nf[i] = nf;
+        if (c->pf)
+            c->pf[i] = pf;
+    }
+}
+
+int orc_bvh_trace(uint32_t layout, const void* nodes, uint64_t node_count,
+                  const igxrt_prim_record* prims, uint64_t prim_count, const igxrt_ray* rays,
+                  const uint32_t* prev_hit, uint32_t nrays, uint32_t mode, igxrt_hit* out_hits,
+                  uint32_t* out_occluded, uint32_t* node_fetches, uint32_t* prim_fetches,
+                  int threads) {
+    bvh_ctx c;
+    c.layout = layout;
+    c.nodes = nodes;
+    c.nn = node_count;
+    c.prims = prims;
+    c.np = prim_count;
+    c.rays = rays;
+    c.prev = prev_hit;
+    c.mode = mode;
+    c.hits = out_hits;
+    c.occ = out_occluded;
+    c.nf = node_fetches;
+    c.pf = prim_fetches;
+    atomic_init(&c.error, 0);
+    run_parallel(bvh_chunk, &c, nrays, 256, threads);
+    return atomic_load(&c.error) ? -1 : 0;
+}

@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -177,15 +178,27 @@ def cpu_baseline(bvh, batches, budget_s: float = 12.0, layout: int = 0) -> dict:
             n += len(r)
         return n, time.perf_counter() - t0
 
-    stride = max(1, total // 20000)
-    n, dt = run(stride)
-    if dt < budget_s and stride > 1:
-        stride = max(1, int(stride * dt / budget_s))
-        n, dt = run(stride)
+    # estimate on a small strided sample, then either repeat whole passes
+    # until the budget is spent or trace one strided pass of about that length
+    probe = max(1, total // 20000)
+    n0, dt0 = run(probe)
+    full_pass_s = dt0 * total / max(n0, 1)
+    stride = 1 if full_pass_s <= budget_s else int(math.ceil(full_pass_s / budget_s))
+    n = 0
+    dt = 0.0
+    passes = 0
+    while dt < budget_s or passes == 0:
+        k, d = run(stride)
+        n += k
+        dt += d
+        passes += 1
+        if stride > 1:
+            break
+    what = "the whole workload" if stride == 1 else f"every {stride}th ray of each batch"
     return {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"every {stride}th ray of each batch ({n} rays, {dt:.1f} s), "
-                      "oracle BVH traversal over the engine's BVH2, "
-                      "triangle test transcribed from primitive.glsl:239-284"}
+            "sample": f"{passes} pass(es) over {what} ({n} rays, {dt:.1f} s): the oracle's BVH "
+                      "traversal over the engine's BVH2 with the triangle test transcribed from "
+                      "primitive.glsl:239-284"}
 
 
 def linear_loop_rate(tris, batches, max_rays: int = 256) -> float:

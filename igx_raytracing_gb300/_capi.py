@@ -21,6 +21,8 @@ LAYOUT_BVH2 = 0
 LAYOUT_BVH4 = 1
 LAYOUT_COUNT = 2
 TRACE_HOST_MEMORY = 1
+STATIC_SCRATCH_BYTES = 16 << 20
+STATIC_MAX_RAYS = 320000
 
 STATUS = {
     0: "IGXRT_OK",
@@ -101,6 +103,7 @@ PROTOTYPES = [
     ("igxrt_get_launch_params", _st, [_vp, C.POINTER(LaunchParams)]),
     ("igxrt_trace_closest", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _u32, _vp]),
     ("igxrt_trace_any", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _u32, _vp]),
+    ("igxrt_trace_closest_static", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _vp]),
     ("igxrt_fetch_hits", _st, [_vp, _vp, _u32, _vp, _vp]),
     ("igxrt_sync", _st, [_vp, _vp]),
     ("igxrt_count_fetches", _st, [_vp, _vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp]),

@@ -60,6 +60,12 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in,
 igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
                           const igxrt_launch_params& params, cudaStream_t stream);
 
+// Same launch, with the work-queue counter and error word supplied by the
+// caller (device addresses); the counter is not reset here.
+igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
+                                const igxrt_launch_params& params, cudaStream_t stream,
+                                uint32_t* queue, uint32_t* status);
+
 // Next work-queue counter of the context (a ring of kQueueSlots words).
 uint32_t* take_queue_slot(igxrt_context* ctx);
 uint32_t* status_word(igxrt_context* ctx);

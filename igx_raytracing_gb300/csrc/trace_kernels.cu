@@ -154,4 +154,46 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     return IGXRT_OK;
 }
 
+igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
+                                const igxrt_launch_params& p, cudaStream_t stream,
+                                uint32_t* queue, uint32_t* status) {
+    if (req.count == 0)
+        return IGXRT_OK;
+    const igxrt_scene* s = req.scene;
+    KernelFn fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr);
+    const size_t smem = (size_t)p.stack_depth * p.block_size * sizeof(uint32_t);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "occupancy query");
+    if (per_sm < 1)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "launch parameters leave no resident CTA");
+    if (p.ctas_per_sm)
+        per_sm = std::min(per_sm, (int)p.ctas_per_sm);
+    const uint64_t warps_needed = ((uint64_t)req.count + p.packet_size - 1) / p.packet_size;
+    const uint64_t ctas_needed = (warps_needed + p.block_size / 32 - 1) / (p.block_size / 32);
+    const uint32_t grid = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, ctas_needed));
+    KernelArgs a;
+    a.nodes = reinterpret_cast<const float4*>(s->nodes[p.layout]);
+    a.prims = reinterpret_cast<const float4*>(s->prims);
+    a.node_count = s->node_count[p.layout];
+    a.rays = req.rays;
+    a.prev = req.prev;
+    a.count = req.count;
+    a.hits = req.hits;
+    a.occluded = req.occluded;
+    a.node_fetches = req.node_fetches;
+    a.prim_fetches = req.prim_fetches;
+    a.queue = queue;
+    a.status = status;
+    a.packet = p.packet_size;
+    a.sh_depth = p.stack_depth;
+    fn<<<grid, p.block_size, smem, stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "trace kernel launch");
+    return IGXRT_OK;
+}
+
 }  // namespace igxrt

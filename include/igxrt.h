@@ -262,6 +262,33 @@ igxrt_status igxrt_trace_any(igxrt_context* ctx, const igxrt_scene* scene,
                              uint32_t count, uint32_t* occluded, uint32_t flags,
                              void* stream);
 
+/*
+ * Closest hit for host arrays without allocating anything.  This entry point
+ * has no counterpart in the reference: it serves callers that must not call
+ * cudaMalloc while they trace, such as a render loop whose device memory is
+ * budgeted by another allocator or whose frame time cannot absorb the
+ * device-wide synchronisation an allocation may cause.  igxrt_trace_closest
+ * with IGXRT_TRACE_HOST_MEMORY may grow its staging buffer with cudaMalloc;
+ * this call stages through a fixed 16 MiB device array instead
+ * (IGXRT_STATIC_SCRATCH_BYTES, a file-scope __device__ array that every GPU
+ * loading the library keeps until the process exits).
+ *   - count may not exceed IGXRT_STATIC_MAX_RAYS; larger calls return
+ *     IGXRT_ERROR_INVALID_ARGUMENT (with a message in igxrt_last_error) and
+ *     launch nothing.  Split bigger batches across calls.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture begins.
+ *   - All calls share the one array.  Each call clears its work counter and
+ *     error word before launching, and returns only after its hits are back
+ *     in host memory, but calls that overlap on the GPU (from several host
+ *     threads or contexts at once) race on the array: serialise them.
+ * Inputs and outputs are as for igxrt_trace_closest with host arrays.
+ */
+#define IGXRT_STATIC_SCRATCH_BYTES (16u << 20)
+#define IGXRT_STATIC_MAX_RAYS 320000u
+igxrt_status igxrt_trace_closest_static(igxrt_context* ctx, const igxrt_scene* scene,
+                                        const igxrt_ray* rays, const uint32_t* prev_hit,
+                                        uint32_t count, igxrt_hit* hits, void* stream);
+
 /* Copies `count` device hits to host memory and waits for them. */
 igxrt_status igxrt_fetch_hits(igxrt_context* ctx, const igxrt_hit* device_hits,
                               uint32_t count, igxrt_hit* host_hits, void* stream);

@@ -228,7 +228,8 @@ class Context:
         p = LaunchParams()
         check(lib().igxrt_get_launch_params(self._h, C.byref(p)), self._h)
         return {"block_size": p.block_size, "stack_depth": p.stack_depth,
-                "packet_size": p.packet_size, "layout": p.layout, "ctas_per_sm": p.ctas_per_sm}
+                "packet_size": p.packet_size, "layout": p.layout, "ctas_per_sm": p.ctas_per_sm,
+                "refill_lanes": p.refill_lanes}
 
     def set_launch_params(self, **kw) -> None:
         cur = self.launch_params

@@ -54,6 +54,11 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
         out.packet_size = 64;
     if (out.stack_depth == 0 && in.block_size == 0 && in.packet_size == 0)
         out.stack_depth = 16;
+    if (!out.refill_lanes)
+        out.refill_lanes = 8;
+    if (out.refill_lanes > 32)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    format("refill_lanes %u: at most 32", out.refill_lanes));
     if (out.block_size < 32 || out.block_size > 256 || out.block_size % 32)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                     format("block_size %u: use a multiple of 32 up to 256", out.block_size));

@@ -36,29 +36,13 @@ struct KernelArgs {
     uint32_t* status;
     uint32_t packet;
     uint32_t sh_depth;
+    uint32_t refill_lanes;
 };
 
-template <int LAYOUT, bool ANY, bool COUNT>
-__device__ __forceinline__ void trace_ray(const KernelArgs& a, uint32_t i, TraversalStack& st) {
-    const uint32_t prev = a.prev ? __ldg(a.prev + i) : IGXRT_NO_RAY_HIT;
-    const RayState r = load_ray(a.rays, i, prev);
-    BestHit best;
-    best.t = r.tmax_eff;
-    best.u = 0.f;
-    best.v = 0.f;
-    best.prim = 0;  // "prim < best.prim" cannot hold before a first hit
-    best.tcull = cull_limit(best.t);
-    bool occluded = false, ok = true;
-    uint32_t nf = 0, pf = 0;
-    st.sp = 0;
-    if (a.node_count) {
-        if (LAYOUT == IGXRT_LAYOUT_BVH4)
-            ok = traverse_bvh4<ANY, COUNT>(a.nodes, a.prims, r, best, st, occluded, nf, pf);
-        else
-            ok = traverse_bvh2<ANY, COUNT>(a.nodes, a.prims, r, best, st, occluded, nf, pf);
-    }
-    if (!ok)
-        atomicOr(a.status, kStatusStackOverflow);
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void finish_ray(const KernelArgs& a, uint32_t i, const RayState& r,
+                                           const BestHit& best, bool occluded, uint32_t nf,
+                                           uint32_t pf) {
     if (ANY) {
         __stcs(a.occluded + i, occluded ? 1u : 0u);
     } else {
@@ -73,6 +57,14 @@ __device__ __forceinline__ void trace_ray(const KernelArgs& a, uint32_t i, Trave
     }
 }
 
+// Persistent traversal.  Every lane owns one ray at a time; a warp alternates
+// a node phase (each lane descends until it reaches a leaf or finishes) and a
+// leaf phase (each lane tests one leaf), so lanes at the same kind of work
+// execute together.  Between phases, once `refill_lanes` lanes are idle the
+// warp hands them new rays: one atomicAdd on the global queue claims a
+// packet of `packet` ray indices for the warp, and idle lanes take the next
+// indices in lane order (ballot + popc).  Per ray the sequence of node and
+// leaf visits is exactly the host traversal's (oracle/trace_oracle.c).
 template <int LAYOUT, bool ANY, bool COUNT>
 __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
     extern __shared__ uint32_t smem[];
@@ -82,16 +74,73 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
     st.sh_depth = a.sh_depth;
     st.sp = 0;
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lower = (1u << lane) - 1u;
+    uint32_t pk_base = 0, pk_end = 0;  // warp-uniform window of claimed rays
+    bool queue_done = false;           // warp-uniform
+    bool alive = false;
+    uint32_t ray = 0, nf = 0, pf = 0;
+    int32_t next = kRefDone;
+    RayState r;
+    BestHit best;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0)
-            base = atomicAdd(a.queue, a.packet);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= a.count)
-            break;
-        const uint32_t end = min(base + a.packet, a.count);
-        for (uint32_t i = base + lane; i < end; i += 32)
-            trace_ray<LAYOUT, ANY, COUNT>(a, i, st);
+        const uint32_t idle = __ballot_sync(0xffffffffu, !alive);
+        const uint32_t nidle = __popc(idle);
+        if (!queue_done && nidle != 0 && (nidle >= a.refill_lanes || nidle == 32)) {
+            const uint32_t rank = __popc(idle & lower);
+            uint32_t given = 0;
+            while (given < nidle) {
+                if (pk_base >= pk_end) {
+                    uint32_t b = 0;
+                    if (lane == 0)
+                        b = atomicAdd(a.queue, a.packet);
+                    b = __shfl_sync(0xffffffffu, b, 0);
+                    if (b >= a.count) {
+                        queue_done = true;
+                        break;
+                    }
+                    pk_base = b;
+                    pk_end = min(b + a.packet, a.count);
+                }
+                const uint32_t take = min(nidle - given, pk_end - pk_base);
+                if (!alive && rank >= given && rank < given + take) {
+                    ray = pk_base + (rank - given);
+                    r = load_ray(a.rays, ray, a.prev ? __ldg(a.prev + ray) : IGXRT_NO_RAY_HIT);
+                    best.t = r.tmax_eff;
+                    best.u = 0.f;
+                    best.v = 0.f;
+                    best.prim = 0;  // "prim < best.prim" cannot hold before a first hit
+                    best.tcull = cull_limit(best.t);
+                    next = a.node_count ? 0 : kRefDone;
+                    st.sp = 0;
+                    nf = 0;
+                    pf = 0;
+                    alive = true;
+                }
+                given += take;
+                pk_base += take;
+            }
+        }
+        if (__ballot_sync(0xffffffffu, alive) == 0)
+            break;  // only reachable once the queue is drained
+        if (alive) {
+            bool overflow = false;
+            // node phase
+            while (next >= 0 && next != kRefDone)
+                next = visit_node<LAYOUT, COUNT>(a.nodes, next, r, best, st, overflow, nf);
+            bool occluded = false;
+            // leaf phase
+            if (next < 0) {
+                occluded = process_leaf<ANY, COUNT>(a.prims, next, r, best, pf);
+                if (!occluded)
+                    next = st.sp == 0 ? kRefDone : st.pop();
+            }
+            if (overflow)
+                atomicOr(a.status, kStatusStackOverflow);
+            if (occluded || next == kRefDone) {
+                finish_ray<ANY, COUNT>(a, ray, r, best, occluded, nf, pf);
+                alive = false;
+            }
+        }
     }
 }
 
@@ -144,6 +193,7 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     a.status = status_word(ctx);
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
+    a.refill_lanes = p.refill_lanes;
     e = cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "queue reset");
@@ -189,6 +239,7 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
     a.status = status;
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
+    a.refill_lanes = p.refill_lanes;
     fn<<<grid, p.block_size, smem, stream>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess)

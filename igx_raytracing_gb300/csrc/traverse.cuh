@@ -173,52 +173,14 @@ __device__ __forceinline__ bool process_leaf(const float4* __restrict__ prims, i
     return false;
 }
 
-// Returns false if the stack would overflow (malformed BVH); `occluded` is
-// set for any-hit queries.
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool traverse_bvh2(const float4* __restrict__ nodes,
-                                              const float4* __restrict__ prims,
-                                              const RayState& r, BestHit& best,
-                                              TraversalStack& st, bool& occluded, uint32_t& nf,
-                                              uint32_t& pf) {
-    int32_t next = 0;
-    for (;;) {
-        if (next >= 0) {
-            const float4* n = nodes + 4 * (size_t)next;
-            const float4 xy0 = __ldg(n), xy1 = __ldg(n + 1), z01 = __ldg(n + 2);
-            const int4 ch = __ldg(reinterpret_cast<const int4*>(n + 3));
-            if (COUNT)
-                ++nf;
-            float tn0, tn1;
-            const bool h0 = box_hit(r, xy0.x, xy0.y, xy0.z, xy0.w, z01.x, z01.y, best.tcull, tn0);
-            const bool h1 = box_hit(r, xy1.x, xy1.y, xy1.z, xy1.w, z01.z, z01.w, best.tcull, tn1);
-            if (h0 && h1) {
-                const bool first1 = tn1 < tn0;
-                if (st.sp >= kStackCapacityDevice)
-                    return false;
-                st.push(first1 ? ch.x : ch.y);
-                next = first1 ? ch.y : ch.x;
-            } else if (h0) {
-                next = ch.x;
-            } else if (h1) {
-                next = ch.y;
-            } else {
-                if (st.sp == 0)
-                    break;
-                next = st.pop();
-            }
-        } else {
-            if (process_leaf<ANY, COUNT>(prims, next, r, best, pf)) {
-                occluded = true;
-                return true;
-            }
-            if (st.sp == 0)
-                break;
-            next = st.pop();
-        }
-    }
-    return true;
+// 256-bit read-only load (sm_100+): eight floats from a 32-byte aligned address.
+__device__ __forceinline__ void ldg256(const void* p, float4& lo, float4& hi) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w)
+        : "l"(p));
 }
+
+constexpr int32_t kRefDone = 0x7fffffff;  // "stack empty": the traversal is over
 
 struct SlotKey {
     float tn;
@@ -235,69 +197,82 @@ __device__ __forceinline__ void order2(SlotKey& a, SlotKey& b) {
     }
 }
 
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool traverse_bvh4(const float4* __restrict__ nodes,
-                                              const float4* __restrict__ prims,
-                                              const RayState& r, BestHit& best,
-                                              TraversalStack& st, bool& occluded, uint32_t& nf,
-                                              uint32_t& pf) {
-    int32_t next = 0;
-    for (;;) {
-        if (next >= 0) {
-            const float4* n = nodes + 8 * (size_t)next;
-            const float4 lx = __ldg(n), hx = __ldg(n + 1), ly = __ldg(n + 2), hy = __ldg(n + 3);
-            const float4 lz = __ldg(n + 4), hz = __ldg(n + 5);
-            const int4 ch = __ldg(reinterpret_cast<const int4*>(n + 6));
-            if (COUNT)
-                ++nf;
-            SlotKey k0, k1, k2, k3;
-            uint32_t m = 0;
-            float tn;
-            uint32_t h = box_hit(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, best.tcull, tn);
-            m += h;
-            k0 = {h ? tn : INFINITY, ch.x, 0u};
-            h = box_hit(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, best.tcull, tn);
-            m += h;
-            k1 = {h ? tn : INFINITY, ch.y, 1u};
-            h = box_hit(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, best.tcull, tn);
-            m += h;
-            k2 = {h ? tn : INFINITY, ch.z, 2u};
-            h = box_hit(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, best.tcull, tn);
-            m += h;
-            k3 = {h ? tn : INFINITY, ch.w, 3u};
-            if (m == 0) {
-                if (st.sp == 0)
-                    break;
-                next = st.pop();
-                continue;
-            }
-            // Sort (tnear, slot) ascending; missed slots carry +inf and sort
-            // last (a hit's tnear is at most the finite cull limit).
-            order2(k0, k1);
-            order2(k2, k3);
-            order2(k0, k2);
-            order2(k1, k3);
-            order2(k1, k2);
-            if (st.sp + m - 1 > kStackCapacityDevice)
-                return false;
-            if (m > 3)
-                st.push(k3.child);
-            if (m > 2)
-                st.push(k2.child);
-            if (m > 1)
-                st.push(k1.child);
-            next = k0.child;
-        } else {
-            if (process_leaf<ANY, COUNT>(prims, next, r, best, pf)) {
-                occluded = true;
-                return true;
-            }
-            if (st.sp == 0)
-                break;
-            next = st.pop();
+// One interior-node visit in the kernels' order: test the children, descend
+// into the nearer hit child and push the other.  Returns the next reference
+// (a node, a leaf, or kRefDone), or sets `overflow`.
+template <int LAYOUT, bool COUNT>
+__device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, int32_t node,
+                                              const RayState& r, const BestHit& best,
+                                              TraversalStack& st, bool& overflow, uint32_t& nf) {
+    if (COUNT)
+        ++nf;
+    if (LAYOUT == IGXRT_LAYOUT_BVH4) {
+        const float4* n = nodes + 8 * (size_t)node;
+        float4 lx, hx, ly, hy, lz, hz, c, unused;
+        ldg256(n, lx, hx);
+        ldg256(n + 2, ly, hy);
+        ldg256(n + 4, lz, hz);
+        ldg256(n + 6, c, unused);
+        const int4 ch = make_int4(__float_as_int(c.x), __float_as_int(c.y), __float_as_int(c.z),
+                                  __float_as_int(c.w));
+        float tn;
+        uint32_t h, m = 0;
+        h = box_hit(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, best.tcull, tn);
+        m += h;
+        SlotKey k0 = {h ? tn : INFINITY, ch.x, 0u};
+        h = box_hit(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, best.tcull, tn);
+        m += h;
+        SlotKey k1 = {h ? tn : INFINITY, ch.y, 1u};
+        h = box_hit(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, best.tcull, tn);
+        m += h;
+        SlotKey k2 = {h ? tn : INFINITY, ch.z, 2u};
+        h = box_hit(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, best.tcull, tn);
+        m += h;
+        SlotKey k3 = {h ? tn : INFINITY, ch.w, 3u};
+        if (m == 0)
+            return st.sp == 0 ? kRefDone : st.pop();
+        // (tnear, slot) ascending; missed slots carry +inf and sort last (a
+        // hit's tnear is at most the finite cull limit)
+        order2(k0, k1);
+        order2(k2, k3);
+        order2(k0, k2);
+        order2(k1, k3);
+        order2(k1, k2);
+        if (st.sp + m - 1 > kStackCapacityDevice) {
+            overflow = true;
+            return kRefDone;
         }
+        if (m > 3)
+            st.push(k3.child);
+        if (m > 2)
+            st.push(k2.child);
+        if (m > 1)
+            st.push(k1.child);
+        return k0.child;
+    } else {
+        const float4* n = nodes + 4 * (size_t)node;
+        float4 xy0, xy1, z01, c;
+        ldg256(n, xy0, xy1);
+        ldg256(n + 2, z01, c);
+        const int32_t c0 = __float_as_int(c.x), c1 = __float_as_int(c.y);
+        float tn0, tn1;
+        const bool h0 = box_hit(r, xy0.x, xy0.y, xy0.z, xy0.w, z01.x, z01.y, best.tcull, tn0);
+        const bool h1 = box_hit(r, xy1.x, xy1.y, xy1.z, xy1.w, z01.z, z01.w, best.tcull, tn1);
+        if (h0 && h1) {
+            const bool first1 = tn1 < tn0;
+            if (st.sp >= kStackCapacityDevice) {
+                overflow = true;
+                return kRefDone;
+            }
+            st.push(first1 ? c0 : c1);
+            return first1 ? c1 : c0;
+        }
+        if (h0)
+            return c0;
+        if (h1)
+            return c1;
+        return st.sp == 0 ? kRefDone : st.pop();
     }
-    return true;
 }
 
 }  // namespace igxrt

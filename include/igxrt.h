@@ -233,10 +233,13 @@ typedef struct igxrt_launch_params {
     uint32_t block_size;  /* threads per CTA: 64, 128 or 256 */
     uint32_t stack_depth; /* shared-memory stack entries per thread: 8, 16 or 32;
                              deeper entries spill to local memory */
-    uint32_t packet_size; /* rays taken per queue fetch: 32, 64 or 128 */
+    uint32_t packet_size; /* rays a warp takes per queue fetch before it starts
+                             refilling single lanes: a multiple of 32 */
     uint32_t layout;      /* IGXRT_LAYOUT_* */
     uint32_t ctas_per_sm; /* persistent CTAs per SM, 0 = as many as fit */
-    uint32_t reserved[3];
+    uint32_t refill_lanes;/* a warp refetches rays once this many of its lanes
+                             are idle (1..32); 0 = 8 */
+    uint32_t reserved[2];
 } igxrt_launch_params;
 
 igxrt_status igxrt_set_launch_params(igxrt_context* ctx, const igxrt_launch_params* p);

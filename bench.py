@@ -10,6 +10,9 @@ Workloads (seeded synthetic inputs, no dataset):
   small         4,096-triangle heightfield, 256x256 primaries.
   incoherent    2,097,152 random triangles, 4,194,304 incoherent rays.
   incoherent1m  1,048,576 random triangles, 4,194,304 incoherent rays.
+  batch         64 random-triangle scenes (1K-512K triangles, 4K-2M rays each):
+                one autotuned, graph-captured persistent launch vs 64
+                sequential plain launches.
 
 value: Mrays/s over all rays of a step, inputs resident in device memory,
 CUDA-event time per step (L2 flushed between steps).  e2e: the same rays
@@ -436,16 +439,312 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     print(json.dumps(line), flush=True)
 
 
+def run_batch_bench(args, rank: int, world: int, local_rank: int):
+    """64 scenes (triangles log-uniform in [1K, 512K]) with ray batches
+    log-uniform in [4K, 2M] (half pinhole primaries, half incoherent): one
+    autotuned, graph-captured persistent launch against 64 sequential plain
+    launches of the same items on one stream."""
+    import torch
+
+    import igx_raytracing_gb300 as igx
+    from igx_raytracing_gb300 import BVH, scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = igx.Context(local_rank)
+    ntris, nrays = scenes.workload_batch_plan(64)
+    t0 = time.perf_counter()
+    items, host_rays, bvhs = [], [], []
+    for i, (nt, nr) in enumerate(zip(ntris, nrays)):
+        tris = scenes.random_triangles(int(nt), scenes.seed_for(4, i))
+        bvh = BVH.build(tris)
+        scene = ctx.create_scene(bvh=bvh)
+        rays = scenes.batch_rays(i, int(nr))
+        d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+        out = torch.empty((len(rays), 4), dtype=torch.float32, device=dev)
+        items.append((scene, d_rays, None, out, 0))
+        host_rays.append(rays)
+        bvhs.append(bvh)
+    setup_s = time.perf_counter() - t0
+    total_rays = int(sum(len(r) for r in host_rays))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    t0 = time.perf_counter()
+    tuned, tuned_ms = ctx.autotune(items, reps=2, force=True)
+    tune_s = time.perf_counter() - t0
+    plain_params = ctx.launch_params
+
+    def timed(fn, steps):
+        ts = []
+        for s in range(steps):
+            flush.fill_(float(s))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return ts
+
+    def sequential():
+        for scene, d_rays, _, out, _ in items:
+            ctx.trace_closest(scene, d_rays, None, out=out)
+
+    batch = ctx.create_batch(items, params=tuned)
+    for _ in range(args.warmup):
+        sequential()
+        batch.launch()
+    torch.cuda.synchronize()
+    seq_ms = statistics.mean(timed(sequential, args.steps))
+    ctx.set_launch_params(**tuned)
+    seq_tuned_ms = statistics.mean(timed(sequential, args.steps))
+    ctx.set_launch_params(**plain_params)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    bat = timed(batch.launch, args.steps)
+    clk = clocks.stop()
+    bat_ms = statistics.mean(bat)
+    ctx.sync()
+    # the batch's results equal the plain launches' (checked bit for bit here
+    # on a few items; the test suite checks every item)
+    # (compared as integers: a miss stores prim 0xFFFFFFFF, a NaN bit pattern)
+    ref = [items[i][3].clone() for i in range(0, 64, 16)]
+    sequential()
+    torch.cuda.synchronize()
+    same = all(torch.equal(ref[k].view(torch.int32), items[i][3].view(torch.int32))
+               for k, i in enumerate(range(0, 64, 16)))
+
+    # roofline over the whole batch launch
+    peaks = measured_peaks()
+    layout = tuned["layout"]
+    bytes_total = 0
+    for (scene, _, _, _, _), rays in zip(items, host_rays):
+        nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
+        bytes_total += algorithmic_bytes(nf, pf, 0, False, layout)
+    achieved = bytes_total / (bat_ms / 1e3) / 1e9
+
+    # e2e: pinned host rays up, one batched launch, hits down
+    pinned = [torch.from_numpy(r.view(np.float32).reshape(-1, 8).copy()).pin_memory() for r in host_rays]
+    hits_host = [torch.empty((len(r), 4), dtype=torch.float32).pin_memory() for r in host_rays]
+
+    def e2e():
+        for (scene, d_rays, _, out, _), hr in zip(items, pinned):
+            d_rays.copy_(hr, non_blocking=True)
+        batch.launch()
+        for (scene, d_rays, _, out, _), hh in zip(items, hits_host):
+            hh.copy_(out, non_blocking=True)
+
+    e2e_ms = statistics.mean(timed(e2e, args.steps))
+    if rank != 0:
+        return
+    value = world * total_rays / (bat_ms / 1e3) / 1e6
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(bat_ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "batch_64_scenes_1k_512k_tris_4k_2m_rays", "scenes": 64,
+                       "triangles": int(ntris.sum()), "rays_per_step": total_rays,
+                       "autotuned": tuned, "autotune_s": round(tune_s, 2),
+                       "setup_s": round(setup_s, 1),
+                       "l2": "256 MiB buffer written between timed steps"},
+            "plain_sequential": {"ms_per_step": round(seq_ms, 4),
+                                 "mrays_s": round(total_rays / (seq_ms / 1e3) / 1e6, 3),
+                                 "params": plain_params},
+            "plain_sequential_tuned": {"ms_per_step": round(seq_tuned_ms, 4),
+                                       "mrays_s": round(total_rays / (seq_tuned_ms / 1e3) / 1e6, 3)},
+            "batched_over_plain": round(seq_ms / bat_ms, 3),
+            "batched_over_plain_tuned": round(seq_tuned_ms / bat_ms, 3),
+            "results_equal_plain": bool(same),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                         "traffic": traffic_from_profiles("batch_64_scenes_1k_512k_tris_4k_2m_rays", "batch"),
+                         "kernel": f"batch_kernel<{'bvh4' if layout else 'bvh2'}>",
+                         "peak_source": peaks["source"]},
+            "e2e": {"value": round(world * total_rays / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
+                    "h2d_bytes_per_step": total_rays * RAY_BYTES,
+                    "d2h_bytes_per_step": total_rays * HIT_BYTES, "ms_per_step": round(e2e_ms, 3)},
+            "gpu_launches": args.steps,
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve_bench(args, rank: int, world: int, local_rank: int):
+    """32 resident scenes (10K-2M triangles), Poisson arrivals at `--rate`
+    requests/s for `--duration` s; each request names a scene, 1K-1M rays
+    (log-uniform), closest or any hit.  The engine's server (admission under a
+    24 GiB cap, continuous batching over 3 streams) against a plain server
+    that traces each request with one plain kernel launch in arrival order,
+    both fed the same request stream."""
+    import queue as pyqueue
+    import threading
+
+    import torch
+
+    import igx_raytracing_gb300 as igx
+    from igx_raytracing_gb300 import BVH, scenes
+
+    torch.cuda.set_device(local_rank)
+    ctx = igx.Context(local_rank)
+    rng = np.random.default_rng(scenes.seed_for(5))
+    ntris = scenes.log_uniform_ints(rng, 10_000, 2_000_000, 32)
+    t0 = time.perf_counter()
+    sc, pools = [], []
+    pool_rays = 1 << 20
+    for i, nt in enumerate(ntris):
+        bvh = BVH.build(scenes.random_triangles(int(nt), scenes.seed_for(5, i)))
+        sc.append(ctx.create_scene(bvh=bvh))
+        r = scenes.batch_rays(1000 + i, pool_rays)
+        pr = torch.empty(pool_rays * 8, dtype=torch.float32).pin_memory().numpy()
+        pr[:] = r.view(np.float32).reshape(-1)
+        pools.append(pr.view(igx.RAY_DTYPE))
+    setup_s = time.perf_counter() - t0
+    # the request stream
+    n_req = int(args.rate * args.duration)
+    gaps = rng.exponential(1.0 / args.rate, n_req)
+    arrivals = np.cumsum(gaps)
+    scene_of = rng.integers(0, 32, n_req)
+    counts = scenes.log_uniform_ints(rng, 1000, 1_000_000, n_req)
+    modes = rng.integers(0, 2, n_req)
+    offsets = rng.integers(0, pool_rays - counts + 1)
+    out_ring = torch.empty(64 << 20, dtype=torch.float32).pin_memory().numpy()  # 256 MiB
+    ring_words = len(out_ring)
+
+    def out_for(k, pos):
+        words = int(counts[k]) * (4 if modes[k] == 0 else 1)
+        pos = (pos + 3) & ~3  # hit records need 16-byte alignment
+        if pos + words > ring_words:
+            pos = 0
+        view = out_ring[pos:pos + words]
+        return (view.view(igx.HIT_DTYPE) if modes[k] == 0 else view.view(np.uint32)), pos + words
+
+    def client(submit):
+        pos = 0
+        start = time.perf_counter()
+        for k in range(n_req):
+            due = start + arrivals[k]
+            while True:
+                d = due - time.perf_counter()
+                if d <= 0:
+                    break
+                if d > 0.0005:
+                    time.sleep(d - 0.0004)
+            out, pos = out_for(k, pos)
+            rays = pools[scene_of[k]][offsets[k]:offsets[k] + counts[k]]
+            submit(k, rays, out)
+
+    # --- engine server ---
+    srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=args.streams)
+    ids = [srv.add_scene(s) for s in sc]
+    # warm-up: a few requests through the server
+    for k in range(8):
+        srv.wait(srv.submit(ids[k], pools[k][:50000], None, k % 2))
+    srv.close()
+    srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=args.streams)
+    ids = [srv.add_scene(s) for s in sc]
+    tickets = [0] * n_req
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+
+    def submit_srv(k, rays, out):
+        tickets[k] = srv.submit(ids[scene_of[k]], rays, None, int(modes[k]), out=out)
+
+    client(submit_srv)
+    srv_lat = np.zeros(n_req)
+    for k, t in enumerate(tickets):
+        w = srv.wait(t)
+        srv_lat[k] = 1e3 * (w["completed"] - w["submitted"])
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    span = st["last_complete"] - st["first_submit"]
+    served = st["rays_completed"] / span / 1e6
+
+    # --- plain server: one plain launch per request, in arrival order ---
+    q = pyqueue.Queue()
+    plain_lat = np.full(n_req, np.nan)
+    errors = []
+
+    def worker():
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            k, rays, out, t_sub = item
+            try:
+                if modes[k] == 0:
+                    ctx.trace_closest(sc[scene_of[k]], rays, None, out=out)
+                else:
+                    ctx.trace_any(sc[scene_of[k]], rays, None, out=out)
+            except Exception as e:  # recorded and reported, never silently dropped
+                errors.append(repr(e))
+            plain_lat[k] = (time.perf_counter() - t_sub) * 1e3
+
+    th = threading.Thread(target=worker)
+    th.start()
+    t_first = time.perf_counter()
+    client(lambda k, rays, out: q.put((k, rays, out, time.perf_counter())))
+    q.put(None)
+    th.join()
+    plain_span = time.perf_counter() - t_first
+
+    def classes(lat):
+        out = {}
+        for name, lo, hi in (("lt10k", 0, 10_000), ("10k_100k", 10_000, 100_000), ("ge100k", 100_000, 1 << 40)):
+            m = (counts >= lo) & (counts < hi)
+            if m.any():
+                out[name] = {"n": int(m.sum()), "p50_ms": round(float(np.percentile(lat[m], 50)), 3),
+                             "p99_ms": round(float(np.percentile(lat[m], 99)), 3)}
+        return out
+
+    plain = {"p50_ms": round(float(np.nanpercentile(plain_lat, 50)), 3),
+             "p99_ms": round(float(np.nanpercentile(plain_lat, 99)), 3),
+             "mrays_s": round(float(counts.sum()) / plain_span / 1e6, 3),
+             "by_size": classes(plain_lat), "errors": len(errors),
+             "first_error": errors[0] if errors else None}
+    if rank != 0:
+        return
+    offered = float(counts.sum()) / float(arrivals[-1]) / 1e6
+    line = {"metric": METRIC, "value": round(served, 3), "unit": UNIT, "n_gpus": world,
+            "steps": n_req, "warmup": 8, "ms_per_step": round(1e3 * span / n_req, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "serve_32_scenes_poisson", "scenes": 32,
+                       "triangles": int(ntris.sum()), "rate_req_s": args.rate,
+                       "duration_s": args.duration, "requests": n_req,
+                       "rays_offered": int(counts.sum()), "offered_mrays_s": round(offered, 3),
+                       "memory_cap_gib": 24, "streams": args.streams, "setup_s": round(setup_s, 1),
+                       "launch": ctx.launch_params},
+            "serving": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                        "mean_ms": round(st["mean_ms"], 3), "max_ms": round(st["max_ms"], 3),
+                        "batches": st["batches"], "requests_per_batch": round(n_req / max(1, st["batches"]), 2),
+                        "peak_memory_gib": round(st["peak_memory_bytes"] / 2**30, 3),
+                        "peak_pending": st["peak_pending"],
+                        "peak_in_flight_batches": st["peak_in_flight_batches"],
+                        "rejected": st["rejected"], "by_size": classes(srv_lat)},
+            "plain_server": plain,
+            "e2e": {"value": round(served, 3), "unit": UNIT,
+                    "h2d_bytes_per_step": int(counts.sum() * RAY_BYTES // n_req),
+                    "d2h_bytes_per_step": int(sum(int(c) * (HIT_BYTES if m == 0 else OCC_BYTES)
+                                                  for c, m in zip(counts, modes)) // n_req)},
+            "gpu_launches": st["batches"],
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="sphere",
-                    choices=["sphere", "small", "incoherent", "incoherent1m"])
+                    choices=["sphere", "small", "incoherent", "incoherent1m", "batch", "serve"])
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--layout", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    ap.add_argument("--streams", type=int, default=2, help="serve: batches in flight")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -459,7 +758,12 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    run_engine(args, rank, world, local_rank)
+    if args.workload == "batch":
+        run_batch_bench(args, rank, world, local_rank)
+    elif args.workload == "serve":
+        run_serve_bench(args, rank, world, local_rank)
+    else:
+        run_engine(args, rank, world, local_rank)
     if world > 1:
         import torch
 

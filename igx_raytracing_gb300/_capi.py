@@ -75,6 +75,19 @@ class LaunchParams(C.Structure):
                 ("refill_lanes", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("rays", C.c_void_p), ("prev_hit", C.c_void_p),
+                ("out", C.c_void_p), ("count", C.c_uint32), ("mode", C.c_uint32)]
+
+
+class TuneOptions(C.Structure):
+    _fields_ = [("reps", C.c_uint32), ("layouts_mask", C.c_uint32), ("cache_path", C.c_char_p),
+                ("class_key", C.c_char_p), ("force", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+
+
+MODE_CLOSEST = 0
+MODE_ANY = 1
+
 _vp = C.c_void_p
 _u32 = C.c_uint32
 _u64 = C.c_uint64
@@ -104,6 +117,13 @@ PROTOTYPES = [
     ("igxrt_trace_closest", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _u32, _vp]),
     ("igxrt_trace_any", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _u32, _vp]),
     ("igxrt_trace_closest_static", _st, [_vp, _vp, _vp, _vp, _u32, _vp, _vp]),
+    ("igxrt_batch_create", _st, [_vp, C.POINTER(BatchItem), _u32, C.POINTER(LaunchParams),
+                                 C.POINTER(_vp)]),
+    ("igxrt_batch_launch", _st, [_vp, _vp]),
+    ("igxrt_batch_destroy", _st, [_vp]),
+    ("igxrt_trace_batch", _st, [_vp, C.POINTER(BatchItem), _u32, _vp]),
+    ("igxrt_autotune", _st, [_vp, C.POINTER(BatchItem), _u32, C.POINTER(TuneOptions),
+                             C.POINTER(LaunchParams), C.POINTER(C.c_float)]),
     ("igxrt_fetch_hits", _st, [_vp, _vp, _u32, _vp, _vp]),
     ("igxrt_sync", _st, [_vp, _vp]),
     ("igxrt_count_fetches", _st, [_vp, _vp, _vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp]),
@@ -145,3 +165,39 @@ def check(status: int, ctx=None, what: str = "") -> None:
         if not msg:
             msg = lib().igxrt_status_string(status).decode()
         raise IgxrtError(status, f"{what}: {msg}" if what else msg)
+
+
+class ServerOptions(C.Structure):
+    _fields_ = [("memory_cap_bytes", C.c_uint64), ("max_batch_rays", C.c_uint32),
+                ("max_batch_requests", C.c_uint32), ("streams", C.c_uint32),
+                ("reserved", C.c_uint32 * 3)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("mode", C.c_uint32), ("count", C.c_uint32),
+                ("reserved", C.c_uint32), ("rays", C.c_void_p), ("prev_hit", C.c_void_p),
+                ("out", C.c_void_p)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("submitted", C.c_double), ("admitted", C.c_double), ("launched", C.c_double),
+                ("completed", C.c_double), ("batch", C.c_uint32), ("status", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("rays_completed", C.c_uint64), ("batches", C.c_uint64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("first_submit", C.c_double), ("last_complete", C.c_double),
+                ("peak_memory_bytes", C.c_uint64), ("peak_pending", C.c_uint32),
+                ("peak_in_flight_batches", C.c_uint32)]
+
+
+PROTOTYPES += [
+    ("igxrt_server_create", _st, [_vp, C.POINTER(ServerOptions), C.POINTER(_vp)]),
+    ("igxrt_server_add_scene", _st, [_vp, _vp, C.POINTER(_u32)]),
+    ("igxrt_server_submit", _st, [_vp, C.POINTER(Request), C.POINTER(_u64)]),
+    ("igxrt_server_wait", _st, [_vp, _u64, C.c_double, C.POINTER(RequestStats)]),
+    ("igxrt_server_get_stats", _st, [_vp, C.POINTER(ServerStats)]),
+    ("igxrt_server_destroy", _st, [_vp]),
+]

@@ -317,6 +317,147 @@ class Context:
     def sync(self, stream=None) -> None:
         check(lib().igxrt_sync(self._h, self._stream(stream, True)), self._h, "sync")
 
+    # -- batched multi-scene queries ---------------------------------------
+    @staticmethod
+    def batch_items(items) -> "C.Array":
+        """items: iterables (scene, rays, prev_hit or None, out, mode) of CUDA
+        tensors; mode 0 = closest (out: (n,4) float32), 1 = any (out: n int32)."""
+        arr = (_capi.BatchItem * max(1, len(items)))()
+        for i, (scene, rays, prev, out, mode) in enumerate(items):
+            assert _is_cuda_tensor(rays) and _is_cuda_tensor(out)
+            arr[i].scene = scene.handle.value
+            arr[i].rays = rays.data_ptr()
+            arr[i].prev_hit = prev.data_ptr() if prev is not None else None
+            arr[i].out = out.data_ptr()
+            arr[i].count = rays.shape[0]
+            arr[i].mode = mode
+        return arr
 
-__all__ = ["BVH", "Context", "Scene", "IgxrtError", "as_rays", "as_triangles", "make_rays",
-           "LAYOUT_BVH2", "LAYOUT_BVH4"]
+    def trace_batch(self, items, stream=None) -> None:
+        """One persistent launch over all items (no graph)."""
+        arr = self.batch_items(items)
+        check(lib().igxrt_trace_batch(self._h, arr, len(items), self._stream(stream, True)),
+              self._h, "trace_batch")
+
+    def create_batch(self, items, params: Optional[dict] = None) -> "Batch":
+        arr = self.batch_items(items)
+        p = None
+        if params is not None:
+            p = LaunchParams()
+            for k, v in params.items():
+                setattr(p, k, int(v))
+        h = C.c_void_p()
+        check(lib().igxrt_batch_create(self._h, arr, len(items), C.byref(p) if p is not None else None,
+                                       C.byref(h)), self._h, "batch_create")
+        return Batch(self, h.value, items)
+
+    def autotune(self, items, reps: int = 3, layouts=None, cache_path: Optional[str] = None,
+                 class_key: Optional[str] = None, force: bool = False):
+        """Times candidate launch parameters on the items; returns (params, ms)."""
+        arr = self.batch_items(items)
+        o = _capi.TuneOptions()
+        o.reps = reps
+        o.layouts_mask = 0 if layouts is None else sum(1 << int(l) for l in layouts)
+        o.cache_path = cache_path.encode() if cache_path else None
+        o.class_key = class_key.encode() if class_key else None
+        o.force = 1 if force else 0
+        p = LaunchParams()
+        ms = C.c_float()
+        check(lib().igxrt_autotune(self._h, arr, len(items), C.byref(o), C.byref(p), C.byref(ms)),
+              self._h, "autotune")
+        return ({"block_size": p.block_size, "stack_depth": p.stack_depth,
+                 "packet_size": p.packet_size, "layout": p.layout, "ctas_per_sm": p.ctas_per_sm,
+                 "refill_lanes": p.refill_lanes}, ms.value)
+
+
+class Server:
+    """igxrt_server: resident scenes, admission by device memory, continuous
+    batching.  Host arrays passed to submit() are kept referenced until the
+    request has been waited for."""
+
+    def __init__(self, ctx: Context, memory_cap_bytes: int = 0, max_batch_rays: int = 0,
+                 max_batch_requests: int = 0, streams: int = 0):
+        o = _capi.ServerOptions()
+        o.memory_cap_bytes, o.max_batch_rays = memory_cap_bytes, max_batch_rays
+        o.max_batch_requests, o.streams = max_batch_requests, streams
+        h = C.c_void_p()
+        check(lib().igxrt_server_create(ctx.handle, C.byref(o), C.byref(h)), ctx.handle,
+              "server_create")
+        self.ctx = ctx
+        self._h = h
+        self._keep = {}
+
+    def add_scene(self, scene: Scene) -> int:
+        sid = C.c_uint32()
+        check(lib().igxrt_server_add_scene(self._h, scene.handle, C.byref(sid)), what="add_scene")
+        return sid.value
+
+    def submit(self, scene_id: int, rays, prev_hit=None, mode: int = 0, out=None) -> int:
+        r = as_rays(rays)
+        prev = None if prev_hit is None else np.ascontiguousarray(prev_hit, dtype=np.uint32)
+        if out is None:
+            out = np.empty(len(r), dtype=HIT_DTYPE) if mode == 0 else np.empty(len(r), dtype=np.uint32)
+        q = _capi.Request()
+        q.scene_id, q.mode, q.count = scene_id, mode, len(r)
+        q.rays = r.ctypes.data if len(r) else None
+        q.prev_hit = prev.ctypes.data if prev is not None else None
+        q.out = out.ctypes.data if len(r) else None
+        t = C.c_uint64()
+        check(lib().igxrt_server_submit(self._h, C.byref(q), C.byref(t)), what="server_submit")
+        self._keep[t.value] = (r, prev, out)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> dict:
+        s = _capi.RequestStats()
+        st = lib().igxrt_server_wait(self._h, ticket, timeout, C.byref(s))
+        if st != 0:
+            raise IgxrtError(st, f"request {ticket}")
+        kept = self._keep.pop(ticket, None)
+        return {"submitted": s.submitted, "admitted": s.admitted, "launched": s.launched,
+                "completed": s.completed, "batch": s.batch,
+                "out": kept[2] if kept is not None else None}
+
+    def stats(self) -> dict:
+        s = _capi.ServerStats()
+        check(lib().igxrt_server_get_stats(self._h, C.byref(s)), what="server_stats")
+        return {f: getattr(s, f) for f, _ in _capi.ServerStats._fields_}
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().igxrt_server_destroy(self._h)
+            self._h = C.c_void_p()
+        self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """igxrt_batch: an item table plus a captured CUDA graph, replayed by launch()."""
+
+    def __init__(self, ctx: Context, handle: int, items):
+        self.ctx = ctx
+        self._h = C.c_void_p(handle)
+        self._items = items  # keep the tensors alive while the graph may run
+
+    def launch(self, stream=None) -> None:
+        check(lib().igxrt_batch_launch(self._h, Context._stream(stream, True)), self.ctx.handle,
+              "batch_launch")
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            lib().igxrt_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+__all__ = ["BVH", "Batch", "Context", "Scene", "Server", "IgxrtError", "as_rays", "as_triangles",
+           "make_rays", "LAYOUT_BVH2", "LAYOUT_BVH4"]

@@ -21,7 +21,8 @@ LIB_PATH = os.path.join(PKG_DIR, "libigxrt.so")
 INCLUDE = os.path.join(REPO_DIR, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["bvh_build.cpp", "capi.cpp", "trace_kernels.cu", "static_scratch.cu"]
+SOURCES = ["bvh_build.cpp", "capi.cpp", "autotune.cpp", "server.cpp", "trace_kernels.cu",
+           "batch.cu", "static_scratch.cu"]
 HEADERS = ["internal.h", "engine.h", "traverse.cuh"]
 
 

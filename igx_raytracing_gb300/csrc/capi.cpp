@@ -81,9 +81,11 @@ namespace {
 
 bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
 
+}  // namespace
+
 // Rejects host pointers passed without IGXRT_TRACE_HOST_MEMORY: a kernel
 // would fault on them.
-bool device_accessible(const void* p) {
+bool igxrt::device_accessible(const void* p) {
     if (!p)
         return true;
     cudaPointerAttributes attr;
@@ -94,6 +96,8 @@ bool device_accessible(const void* p) {
     return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged ||
            (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr);
 }
+
+namespace {
 
 igxrt_status check_scene(igxrt_context* ctx, const igxrt_scene* scene) {
     if (!scene)
@@ -262,6 +266,9 @@ igxrt_status igxrt_create(int device, igxrt_context** out) {
     if (!ctx)
         return IGXRT_ERROR_OUT_OF_MEMORY;
     ctx->device = device;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess)
+        ctx->device_name = prop.name;
     if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaMalloc(&ctx->d_words, (kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess ||
         cudaMemset(ctx->d_words, 0, (kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess) {
@@ -283,6 +290,12 @@ igxrt_status igxrt_destroy(igxrt_context* ctx) {
     {
         DeviceGuard guard(ctx->device);
         cudaDeviceSynchronize();
+        if (ctx->d_batch) {
+            cudaFree(ctx->d_batch);
+            for (uint32_t i = 0; i < kBatchSlots; ++i)
+                if (ctx->batch_events[i])
+                    cudaEventDestroy(ctx->batch_events[i]);
+        }
         if (ctx->d_stage)
             cudaFree(ctx->d_stage);
         if (ctx->d_words)

@@ -5,13 +5,25 @@
 
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "internal.h"
+
+namespace igxrt {
+// Ring of item tables used by igxrt_trace_batch.
+constexpr uint32_t kBatchSlots = 16;
+constexpr uint32_t kBatchSlotItems = 4096;
+}  // namespace igxrt
 
 struct igxrt_context {
     int device = 0;
     int sm_count = 0;
+    std::string device_name;
     std::string last_error;
+    // igxrt_trace_batch item tables and the events guarding their reuse.
+    void* d_batch = nullptr;
+    cudaEvent_t batch_events[igxrt::kBatchSlots] = {};
+    uint32_t next_batch_slot = 0;
     // Device words: kQueueSlots work-queue counters, then the error word.
     uint32_t* d_words = nullptr;
     uint32_t next_slot = 0;
@@ -66,9 +78,33 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
                                 const igxrt_launch_params& params, cudaStream_t stream,
                                 uint32_t* queue, uint32_t* status);
 
+// Device descriptor of one batch item (see batch.cu).
+struct BatchItemDev {
+    const float4* nodes;
+    const float4* prims;
+    const igxrt_ray* rays;
+    const uint32_t* prev;
+    void* out;
+    uint32_t count;
+    uint32_t mode;
+    uint32_t node_count;
+    uint32_t packet_begin;  // first packet of this item in the batch's packet space
+};
+
+igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,
+                               const igxrt_launch_params& p, std::vector<BatchItemDev>& table,
+                               uint32_t& total_packets, uint64_t& total_rays);
+igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint32_t count,
+                          uint32_t total_packets, uint64_t total_rays, const igxrt_launch_params& p,
+                          uint32_t* queue, cudaStream_t stream);
+
 // Next work-queue counter of the context (a ring of kQueueSlots words).
 uint32_t* take_queue_slot(igxrt_context* ctx);
 uint32_t* status_word(igxrt_context* ctx);
+
+// True when a kernel may dereference p: device, managed or mapped pinned
+// memory (NULL counts as accessible).  Pageable host memory is not.
+bool device_accessible(const void* p);
 
 // Makes ctx->device current for the lifetime of the guard.
 class DeviceGuard {

@@ -292,6 +292,125 @@ igxrt_status igxrt_trace_closest_static(igxrt_context* ctx, const igxrt_scene* s
                                         const igxrt_ray* rays, const uint32_t* prev_hit,
                                         uint32_t count, igxrt_hit* hits, void* stream);
 
+/* ---- Batched multi-scene queries ------------------------------------------ */
+
+#define IGXRT_MODE_CLOSEST 0u
+#define IGXRT_MODE_ANY 1u
+
+/* One ray batch of a batched launch.  All pointers are device memory. */
+typedef struct igxrt_batch_item {
+    const igxrt_scene* scene;
+    const igxrt_ray* rays;
+    const uint32_t* prev_hit; /* may be NULL */
+    void* out;                /* igxrt_hit[count] (closest) or uint32_t[count] (any) */
+    uint32_t count;
+    uint32_t mode;            /* IGXRT_MODE_CLOSEST or IGXRT_MODE_ANY */
+} igxrt_batch_item;
+
+typedef struct igxrt_batch igxrt_batch;
+
+/*
+ * Prepares one persistent launch over `count` items (different scenes, uneven
+ * ray counts, closest and any queries mixed): the rays of all items form one
+ * work queue of packets, so the GPU stays full across item boundaries.  The
+ * item table is uploaded once and the queue reset plus the kernel are
+ * captured in a CUDA graph; igxrt_batch_launch replays it.  params NULL
+ * takes the context's launch parameters.  Results are identical to tracing
+ * each item on its own.
+ */
+igxrt_status igxrt_batch_create(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,
+                                const igxrt_launch_params* params, igxrt_batch** out);
+igxrt_status igxrt_batch_launch(igxrt_batch* batch, void* stream);
+igxrt_status igxrt_batch_destroy(igxrt_batch* batch);
+
+/* The same launch without a graph: uploads the item table on `stream` into
+ * the context's batch staging and launches once. */
+igxrt_status igxrt_trace_batch(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,
+                               void* stream);
+
+/* Autotuner: times candidate launch parameters (node layout, block size,
+ * shared stack depth, packet size, refill threshold) on the given items and
+ * returns the fastest.  With a cache file, results are stored under
+ * (GPU name, class key) and reused without timing. */
+typedef struct igxrt_tune_options {
+    uint32_t reps;         /* timed repetitions per candidate, 0 = 3 */
+    uint32_t layouts_mask; /* bit per IGXRT_LAYOUT_*, 0 = all */
+    const char* cache_path;/* NULL = no cache */
+    const char* class_key; /* cache key of this workload class, NULL = derived */
+    uint32_t force;        /* 1 = ignore a cached entry */
+    uint32_t reserved[3];
+} igxrt_tune_options;
+
+igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,
+                            const igxrt_tune_options* opts, igxrt_launch_params* best,
+                            float* best_ms);
+
+/* ---- Serving: resident scenes, admission by memory, continuous batching ---- */
+
+typedef struct igxrt_server igxrt_server;
+
+typedef struct igxrt_server_options {
+    uint64_t memory_cap_bytes;   /* device bytes for the ray, prev_hit and result
+                                    buffers of admitted requests; 0 = 24 GiB */
+    uint32_t max_batch_rays;     /* rays coalesced into one launch, 0 = 4M */
+    uint32_t max_batch_requests; /* requests per launch, 0 = 1024 (at most 4096) */
+    uint32_t streams;            /* batches in flight at once, 0 = 3 */
+    uint32_t reserved[3];
+} igxrt_server_options;
+
+/* A ray-query request.  The arrays are host memory owned by the caller and
+ * must stay valid until the request completes; pinned memory makes the
+ * copies asynchronous. */
+typedef struct igxrt_request {
+    uint32_t scene_id;        /* from igxrt_server_add_scene */
+    uint32_t mode;            /* IGXRT_MODE_CLOSEST or IGXRT_MODE_ANY */
+    uint32_t count;
+    uint32_t reserved;
+    const igxrt_ray* rays;
+    const uint32_t* prev_hit; /* may be NULL */
+    void* out;                /* igxrt_hit[count] or uint32_t[count] */
+} igxrt_request;
+
+/* Timestamps in seconds since the server started (host steady clock). */
+typedef struct igxrt_request_stats {
+    double submitted;
+    double admitted;  /* its buffers were reserved under the cap */
+    double launched;  /* its batch was queued on a stream */
+    double completed; /* its results were in host memory */
+    uint32_t batch;   /* sequence number of the launch that carried it */
+    uint32_t status;  /* igxrt_status of the request */
+} igxrt_request_stats;
+
+typedef struct igxrt_server_stats {
+    uint64_t submitted, completed, rejected;
+    uint64_t rays_completed;
+    uint64_t batches;
+    double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> completed */
+    double first_submit, last_complete;     /* seconds since start */
+    uint64_t peak_memory_bytes;             /* peak reserved under the cap */
+    uint32_t peak_pending;                  /* most requests waiting for admission */
+    uint32_t peak_in_flight_batches;
+} igxrt_server_stats;
+
+/* Starts a server on the context's device (one scheduler thread).  The
+ * context must not be used by other threads while the server runs. */
+igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options* opts,
+                                 igxrt_server** out);
+/* Registers a resident scene; it must outlive the server. */
+igxrt_status igxrt_server_add_scene(igxrt_server* server, const igxrt_scene* scene,
+                                    uint32_t* scene_id);
+/* Queues a request and returns at once.  A request whose buffers can never
+ * fit the memory cap is refused with IGXRT_ERROR_ADMISSION; others wait in
+ * FIFO order until their buffers fit. */
+igxrt_status igxrt_server_submit(igxrt_server* server, const igxrt_request* req, uint64_t* ticket);
+/* Blocks until the request completes (IGXRT_ERROR_TIMEOUT after timeout_s,
+ * < 0 = no limit); stats may be NULL. */
+igxrt_status igxrt_server_wait(igxrt_server* server, uint64_t ticket, double timeout_s,
+                               igxrt_request_stats* stats);
+igxrt_status igxrt_server_get_stats(igxrt_server* server, igxrt_server_stats* stats);
+/* Finishes all queued work, then stops the scheduler and frees its memory. */
+igxrt_status igxrt_server_destroy(igxrt_server* server);
+
 /* Copies `count` device hits to host memory and waits for them. */
 igxrt_status igxrt_fetch_hits(igxrt_context* ctx, const igxrt_hit* device_hits,
                               uint32_t count, igxrt_hit* host_hits, void* stream);

@@ -282,6 +282,7 @@ def run_engine(args, rank: int, world: int, local_rank: int):
 
     import igx_raytracing_gb300 as igx
     from igx_raytracing_gb300 import BVH
+    from igx_raytracing_gb300.dist import max_over_ranks
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -345,11 +346,9 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     ctx.sync()
     launch_ms = np.array([[ev[s][i][0].elapsed_time(ev[s][i][1]) for i in range(nb)]
                           for s in range(args.steps)])
-    step_ms = float(launch_ms.sum(axis=1).mean())
-    if world > 1:
-        t = torch.tensor([step_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms = float(t.item())
+    # each rank traces its own replica of the workload (weak scaling); the
+    # slowest rank defines the step time
+    step_ms = max_over_ranks(float(launch_ms.sum(axis=1).mean()), dev)
     value = world * total_rays / (step_ms / 1e3) / 1e6
 
     # roofline: algorithmic bytes per launch from the instrumented kernel
@@ -406,11 +405,7 @@ def run_engine(args, rank: int, world: int, local_rank: int):
         t0 = time.perf_counter()
         e2e_step()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_ms = 1000 * statistics.mean(e2e_times)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(1000 * statistics.mean(e2e_times), dev)
     e2e_value = world * total_rays / (e2e_ms / 1e3) / 1e6
 
     if rank != 0:
@@ -576,9 +571,6 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
     24 GiB cap, continuous batching over 3 streams) against a plain server
     that traces each request with one plain kernel launch in arrival order,
     both fed the same request stream."""
-    import queue as pyqueue
-    import threading
-
     import torch
 
     import igx_raytracing_gb300 as igx
@@ -633,60 +625,44 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
             rays = pools[scene_of[k]][offsets[k]:offsets[k] + counts[k]]
             submit(k, rays, out)
 
-    # --- engine server ---
-    srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=args.streams)
-    ids = [srv.add_scene(s) for s in sc]
-    # warm-up: a few requests through the server
-    for k in range(8):
-        srv.wait(srv.submit(ids[k], pools[k][:50000], None, k % 2))
-    srv.close()
-    srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=args.streams)
-    ids = [srv.add_scene(s) for s in sc]
-    tickets = [0] * n_req
-    clocks = ClockSampler(local_rank)
-    clocks.start()
+    def serve_pass(streams: int, max_batch_requests: int, with_clocks: bool):
+        srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=streams,
+                         max_batch_requests=max_batch_requests)
+        ids = [srv.add_scene(s) for s in sc]
+        for k in range(8):  # warm-up requests
+            srv.wait(srv.submit(ids[k], pools[k][:50000], None, k % 2))
+        srv.close()
+        srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=streams,
+                         max_batch_requests=max_batch_requests)
+        ids = [srv.add_scene(s) for s in sc]
+        tickets = [0] * n_req
+        clocks = ClockSampler(local_rank)
+        if with_clocks:
+            clocks.start()
 
-    def submit_srv(k, rays, out):
-        tickets[k] = srv.submit(ids[scene_of[k]], rays, None, int(modes[k]), out=out)
+        def submit_srv(k, rays, out):
+            tickets[k] = srv.submit(ids[scene_of[k]], rays, None, int(modes[k]), out=out)
 
-    client(submit_srv)
-    srv_lat = np.zeros(n_req)
-    for k, t in enumerate(tickets):
-        w = srv.wait(t)
-        srv_lat[k] = 1e3 * (w["completed"] - w["submitted"])
-    clk = clocks.stop()
-    st = srv.stats()
-    srv.close()
+        client(submit_srv)
+        lat = np.zeros(n_req)
+        for k, t in enumerate(tickets):
+            w = srv.wait(t)
+            lat[k] = 1e3 * (w["completed"] - w["submitted"])
+        clk = clocks.stop() if with_clocks else None
+        st = srv.stats()
+        srv.close()
+        return st, lat, clk
+
+    # the client thread spins between arrivals: keep its GIL slices short
+    sys.setswitchinterval(1e-4)
+    # engine: continuous batching, `streams` batches in flight
+    st, srv_lat, clk = serve_pass(args.streams, 0, True)
     span = st["last_complete"] - st["first_submit"]
     served = st["rays_completed"] / span / 1e6
-
-    # --- plain server: one plain launch per request, in arrival order ---
-    q = pyqueue.Queue()
-    plain_lat = np.full(n_req, np.nan)
-    errors = []
-
-    def worker():
-        while True:
-            item = q.get()
-            if item is None:
-                return
-            k, rays, out, t_sub = item
-            try:
-                if modes[k] == 0:
-                    ctx.trace_closest(sc[scene_of[k]], rays, None, out=out)
-                else:
-                    ctx.trace_any(sc[scene_of[k]], rays, None, out=out)
-            except Exception as e:  # recorded and reported, never silently dropped
-                errors.append(repr(e))
-            plain_lat[k] = (time.perf_counter() - t_sub) * 1e3
-
-    th = threading.Thread(target=worker)
-    th.start()
-    t_first = time.perf_counter()
-    client(lambda k, rays, out: q.put((k, rays, out, time.perf_counter())))
-    q.put(None)
-    th.join()
-    plain_span = time.perf_counter() - t_first
+    # plain: the same native server launching one request at a time, in
+    # arrival order, one launch in flight (no coalescing, no overlap)
+    pst, plain_lat, _ = serve_pass(1, 1, False)
+    plain_span = pst["last_complete"] - pst["first_submit"]
 
     def classes(lat):
         out = {}
@@ -697,11 +673,10 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
                              "p99_ms": round(float(np.percentile(lat[m], 99)), 3)}
         return out
 
-    plain = {"p50_ms": round(float(np.nanpercentile(plain_lat, 50)), 3),
-             "p99_ms": round(float(np.nanpercentile(plain_lat, 99)), 3),
-             "mrays_s": round(float(counts.sum()) / plain_span / 1e6, 3),
-             "by_size": classes(plain_lat), "errors": len(errors),
-             "first_error": errors[0] if errors else None}
+    plain = {"p50_ms": round(pst["p50_ms"], 3), "p99_ms": round(pst["p99_ms"], 3),
+             "mrays_s": round(pst["rays_completed"] / plain_span / 1e6, 3),
+             "batches": pst["batches"], "by_size": classes(plain_lat),
+             "mode": "same server, one request per launch, one launch in flight"}
     if rank != 0:
         return
     offered = float(counts.sum()) / float(arrivals[-1]) / 1e6

@@ -201,3 +201,17 @@ PROTOTYPES += [
     ("igxrt_server_get_stats", _st, [_vp, C.POINTER(ServerStats)]),
     ("igxrt_server_destroy", _st, [_vp]),
 ]
+
+PROTOTYPES += [
+    ("igxrt_trace_shadow_mask", _st, [_vp, _vp, _vp, _vp, _u32, _u32, _u32, _vp, _u32, _vp]),
+]
+
+# igxrt_camera (64 bytes)
+CAMERA_DTYPE = np.dtype([("eye", "<f4", (3,)), ("width", "<u4"), ("p0", "<f4", (3,)),
+                         ("height", "<u4"), ("p1", "<f4", (3,)), ("jitter_x", "<f4"),
+                         ("p2", "<f4", (3,)), ("jitter_y", "<f4")])
+assert CAMERA_DTYPE.itemsize == 64
+
+PROTOTYPES += [
+    ("igxrt_trace_gbuffer", _st, [_vp, _vp, _vp, _vp, _vp, _u32, _vp]),
+]

@@ -300,6 +300,51 @@ class Context:
     def trace_any(self, scene: Scene, rays, prev_hit=None, stream=None, out=None):
         return self._trace(scene, rays, prev_hit, 1, stream, out)
 
+    def trace_shadow_mask(self, scene: Scene, rays, object_, width: int, height: int,
+                          samples: int, stream=None, out=None):
+        """The reference's shadow pass (nv_all.shadow.comp): ballot words per
+        16x2 tile and sample.  rays: width*height*samples in (sample, y, x)
+        order; object_: width*height primary objects (NO_RAY_HIT = no ray)."""
+        words = ((width + 15) // 16) * ((height + 1) // 2) * samples
+        fn = lib().igxrt_trace_shadow_mask
+        if _is_cuda_tensor(rays):
+            if out is None:
+                out = torch.empty(words, dtype=torch.int32, device=rays.device)
+            check(fn(self._h, scene.handle, rays.data_ptr(), object_.data_ptr(), width, height,
+                     samples, out.data_ptr(), 0, self._stream(stream, True)), self._h, "shadow_mask")
+            return out
+        r = as_rays(rays)
+        obj = np.ascontiguousarray(object_, dtype=np.uint32)
+        if len(r) != width * height * samples or len(obj) != width * height:
+            raise ValueError("rays must be width*height*samples, object width*height")
+        if out is None:
+            out = np.zeros(words, dtype=np.uint32)
+        if words:
+            check(fn(self._h, scene.handle, r.ctypes.data, obj.ctypes.data, width, height, samples,
+                     out.ctypes.data, TRACE_HOST_MEMORY, self._stream(stream, False)), self._h,
+                  "shadow_mask")
+        return out
+
+    def trace_gbuffer(self, scene: Scene, camera, dir_object=None, uv_normal=None, stream=None):
+        """The reference's primary pass (raygen.comp): returns the two
+        (height, width, 4) float32 images dir_object and uv_normal.  camera is
+        a CAMERA_DTYPE record; uv_normal keeps its contents where rays miss."""
+        cam = np.ascontiguousarray(camera, dtype=_capi.CAMERA_DTYPE).reshape(1)
+        w, h = int(cam["width"][0]), int(cam["height"][0])
+        fn = lib().igxrt_trace_gbuffer
+        if dir_object is not None and _is_cuda_tensor(dir_object):
+            check(fn(self._h, scene.handle, cam.ctypes.data, dir_object.data_ptr(),
+                     uv_normal.data_ptr(), 0, self._stream(stream, True)), self._h, "gbuffer")
+            return dir_object, uv_normal
+        if dir_object is None:
+            dir_object = np.zeros((h, w, 4), dtype=np.float32)
+        if uv_normal is None:
+            uv_normal = np.zeros((h, w, 4), dtype=np.float32)
+        check(fn(self._h, scene.handle, cam.ctypes.data, dir_object.ctypes.data,
+                 uv_normal.ctypes.data, TRACE_HOST_MEMORY, self._stream(stream, False)), self._h,
+              "gbuffer")
+        return dir_object, uv_normal
+
     def count_fetches(self, scene: Scene, rays, prev_hit=None, mode: int = 0,
                       layout: int = LAYOUT_BVH2):
         """Node and primitive records the kernel fetches per ray (host arrays)."""

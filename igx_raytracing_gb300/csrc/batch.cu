@@ -37,7 +37,7 @@ template <int LAYOUT>
 __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
     extern __shared__ uint32_t smem[];
     TraversalStack st;
-    st.sh = smem + threadIdx.x;
+    st.sh = reinterpret_cast<uint2*>(smem) + threadIdx.x;
     st.stride = blockDim.x;
     st.sh_depth = a.sh_depth;
     st.sp = 0;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
                 occluded = mode ? process_leaf<true, false>(prims, next, r, best, unused)
                                 : process_leaf<false, false>(prims, next, r, best, unused);
                 if (!occluded)
-                    next = st.sp == 0 ? kRefDone : st.pop();
+                    next = st.pop_live(best.tcull);
             }
             if (overflow)
                 atomicOr(a.status, kStatusStackOverflow);
@@ -206,9 +206,11 @@ igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint3
     if (total_packets == 0)
         return IGXRT_OK;
     BatchFn fn = select_batch_kernel(p.layout);
-    const size_t smem = (size_t)p.stack_depth * p.block_size * sizeof(uint32_t);
+    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    cudaError_t e = allow_smem((const void*)fn, smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "occupancy query");
     if (per_sm < 1)

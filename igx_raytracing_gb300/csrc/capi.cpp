@@ -97,9 +97,7 @@ bool igxrt::device_accessible(const void* p) {
            (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr);
 }
 
-namespace {
-
-igxrt_status check_scene(igxrt_context* ctx, const igxrt_scene* scene) {
+igxrt_status igxrt::check_scene(igxrt_context* ctx, const igxrt_scene* scene) {
     if (!scene)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "scene is NULL");
     if (scene->device != ctx->device)
@@ -108,7 +106,7 @@ igxrt_status check_scene(igxrt_context* ctx, const igxrt_scene* scene) {
     return IGXRT_OK;
 }
 
-igxrt_status grow_stage(igxrt_context* ctx, size_t bytes) {
+igxrt_status igxrt::grow_stage(igxrt_context* ctx, size_t bytes) {
     if (ctx->stage_bytes >= bytes)
         return IGXRT_OK;
     if (ctx->d_stage) {
@@ -132,9 +130,7 @@ igxrt_status grow_stage(igxrt_context* ctx, size_t bytes) {
     return IGXRT_OK;
 }
 
-size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-igxrt_status read_status(igxrt_context* ctx) {
+igxrt_status igxrt::read_status(igxrt_context* ctx) {
     uint32_t word = 0;
     cudaError_t e = cudaMemcpy(&word, status_word(ctx), sizeof(word), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess)
@@ -146,6 +142,10 @@ igxrt_status read_status(igxrt_context* ctx) {
     }
     return IGXRT_OK;
 }
+
+namespace {
+
+size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_ray* rays,
                           const uint32_t* prev, uint32_t count, uint32_t mode, void* out,

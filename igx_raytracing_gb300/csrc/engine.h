@@ -102,6 +102,21 @@ igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint3
 uint32_t* take_queue_slot(igxrt_context* ctx);
 uint32_t* status_word(igxrt_context* ctx);
 
+// Opts a kernel into more than 48 KB of dynamic shared memory when `smem`
+// needs it (the traversal stacks of deep shared stacks and large blocks).
+inline cudaError_t allow_smem(const void* kernel, size_t smem) {
+    if (smem <= 48 * 1024)
+        return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// Scene belongs to the context's device.
+igxrt_status check_scene(igxrt_context* ctx, const igxrt_scene* scene);
+// Grows the context's staging buffer for host-memory calls to `bytes`.
+igxrt_status grow_stage(igxrt_context* ctx, size_t bytes);
+// Reads and clears the context's kernel error word (synchronous).
+igxrt_status read_status(igxrt_context* ctx);
+
 // True when a kernel may dereference p: device, managed or mapped pinned
 // memory (NULL counts as accessible).  Pageable host memory is not.
 bool device_accessible(const void* p);

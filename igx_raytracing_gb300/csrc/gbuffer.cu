@@ -1,0 +1,221 @@
+// gbuffer.cu — the reference's primary pass (raygen.comp) as one kernel:
+// primary-ray generation, closest hit and the shader's two output encodings.
+//
+// Every step follows the shader's binary32 expression order with separately
+// rounded operations: the screen mapping of calculateScreen
+// (res/shaders/camera.glsl:72-87, 113-116), the hit encoding of
+// raygen.comp:39-51, decodeSpheremap / interpolate / encodeNormal
+// (res/shaders/primitive.glsl:85-104, 146-151) for the vertex normal of
+// trace.glsl:48-57.  A warp covers an 8x4 pixel tile so neighbouring
+// primary rays traverse together.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
+#include "engine.h"
+#include "traverse.cuh"
+
+namespace igxrt {
+
+struct GbufferArgs {
+    const float4* nodes;
+    const float4* prims;
+    uint32_t node_count;
+    const igxrt_triangle* tris;
+    igxrt_camera cam;
+    float inv_w, inv_h;
+    uint32_t tiles_x, tiles;
+    float4* dir_object;
+    float4* uv_normal;
+    uint32_t* status;
+    uint32_t sh_depth;
+};
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// decodeSpheremap, primitive.glsl:95-104.
+__device__ __forceinline__ float3 decode_spheremap(uint32_t n) {
+    const float x = __half2float(__ushort_as_half((unsigned short)(n & 0xffffu)));
+    const float y = __half2float(__ushort_as_half((unsigned short)(n >> 16)));
+    // l = dot(vec3(nn, 1), -vec3(nn, -1))
+    const float l = dot3(x, y, 1.0f, -x, -y, 1.0f);
+    const float s = __fsqrt_rn(l);
+    const float sx = __fmul_rn(x, s), sy = __fmul_rn(y, s);
+    // vec3(nn, l) * 2 + vec3(0, 0, -1)
+    return make_float3(__fadd_rn(__fmul_rn(sx, 2.0f), 0.0f), __fadd_rn(__fmul_rn(sy, 2.0f), 0.0f),
+                       __fadd_rn(__fmul_rn(l, 2.0f), -1.0f));
+}
+
+// encodeNormal, primitive.glsl:85-88.
+__device__ __forceinline__ uint2 encode_normal(float3 n) {
+    const float len = __fsqrt_rn(dot3(n.x, n.y, n.z, n.x, n.y, n.z));
+    const float qx = __fdiv_rn(n.x, len), qy = __fdiv_rn(n.y, len), qz = __fdiv_rn(n.z, len);
+    const uint32_t hx = __float2uint_rz(__fmul_rn(__fadd_rn(__fmul_rn(qx, 0.5f), 0.5f), 65535.0f));
+    const uint32_t hy = __float2uint_rz(__fmul_rn(__fadd_rn(__fmul_rn(qy, 0.5f), 0.5f), 65535.0f));
+    const uint32_t hz = __float2uint_rz(__fmul_rn(__fadd_rn(__fmul_rn(qz, 0.5f), 0.5f), 65535.0f));
+    return make_uint2((hx << 16) | hy, hz);
+}
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
+    extern __shared__ uint32_t smem[];
+    TraversalStack st;
+    st.sh = reinterpret_cast<uint2*>(smem) + threadIdx.x;
+    st.stride = blockDim.x;
+    st.sh_depth = a.sh_depth;
+    st.sp = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const igxrt_camera& c = a.cam;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < a.tiles; w += warps) {
+        const uint32_t ty = w / a.tiles_x, tx = w - ty * a.tiles_x;
+        const uint32_t x = tx * 8u + (lane & 7u), y = ty * 4u + (lane >> 3);
+        if (x >= c.width || y >= c.height)
+            continue;
+        // calculatePrimary / calculateScreen
+        const float cx = __fmul_rn(__fadd_rn((float)x, c.jitter_x), a.inv_w);
+        const float cy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn((float)y, c.jitter_y), a.inv_h));
+        float d[3];
+        for (int k = 0; k < 3; ++k) {
+            const float right = __fsub_rn(c.p1[k], c.p0[k]), up = __fsub_rn(c.p2[k], c.p0[k]);
+            const float pos = __fadd_rn(__fadd_rn(c.p0[k], __fmul_rn(cx, right)), __fmul_rn(cy, up));
+            d[k] = __fsub_rn(pos, c.eye[k]);
+        }
+        const float len = __fsqrt_rn(dot3(d[0], d[1], d[2], d[0], d[1], d[2]));
+        const float dx = __fdiv_rn(d[0], len), dy = __fdiv_rn(d[1], len), dz = __fdiv_rn(d[2], len);
+        RayState r;
+        r.ox = c.eye[0];
+        r.oy = c.eye[1];
+        r.oz = c.eye[2];
+        r.dx = dx;
+        r.dy = dy;
+        r.dz = dz;
+        r.ix = __frcp_rn(safe_dir(dx));
+        r.iy = __frcp_rn(safe_dir(dy));
+        r.iz = __frcp_rn(safe_dir(dz));
+        r.oix = __fmul_rn(r.ox, r.ix);
+        r.oiy = __fmul_rn(r.oy, r.iy);
+        r.oiz = __fmul_rn(r.oz, r.iz);
+        r.tmin = 0.f;
+        r.tmin_box = 0.f;
+        r.tmax_eff = IGXRT_NO_HIT;
+        r.prev = IGXRT_NO_RAY_HIT;
+        BestHit best;
+        bool overflow = false;
+        trace_single<LAYOUT, false>(a.nodes, a.prims, a.node_count, r, best, st, overflow);
+        if (overflow)
+            atomicOr(a.status, kStatusStackOverflow);
+        const size_t px = (size_t)y * c.width + x;
+        if (best.t < IGXRT_NO_HIT) {
+            a.dir_object[px] = make_float4(__fmul_rn(dx, best.t), __fmul_rn(dy, best.t),
+                                           __fmul_rn(dz, best.t), __uint_as_float(best.prim));
+            const igxrt_triangle& t = a.tris[best.prim];
+            const float3 n0 = decode_spheremap(t.n0), n1 = decode_spheremap(t.n1),
+                         n2 = decode_spheremap(t.n2);
+            // interpolate(n0, n1, n2, uv): (u*n1 + v*n2) + (1 - u - v)*n0
+            const float u = best.u, v = best.v, bw = __fsub_rn(__fsub_rn(1.0f, u), v);
+            const float3 n = make_float3(
+                __fadd_rn(__fadd_rn(__fmul_rn(u, n1.x), __fmul_rn(v, n2.x)), __fmul_rn(bw, n0.x)),
+                __fadd_rn(__fadd_rn(__fmul_rn(u, n1.y), __fmul_rn(v, n2.y)), __fmul_rn(bw, n0.y)),
+                __fadd_rn(__fadd_rn(__fmul_rn(u, n1.z), __fmul_rn(v, n2.z)), __fmul_rn(bw, n0.z)));
+            const uint2 e = encode_normal(n);
+            a.uv_normal[px] = make_float4(u, v, __uint_as_float(e.x), __uint_as_float(e.y));
+        } else {
+            a.dir_object[px] = make_float4(dx, dy, dz, __uint_as_float(IGXRT_NO_RAY_HIT));
+        }
+    }
+}
+
+}  // namespace igxrt
+
+using namespace igxrt;
+
+extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scene* scene,
+                                            const igxrt_camera* cam, float* dir_object,
+                                            float* uv_normal, uint32_t flags, void* stream_ptr) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    igxrt_status st = check_scene(ctx, scene);
+    if (st != IGXRT_OK)
+        return st;
+    if (!cam || !dir_object || !uv_normal)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "camera and both images must be non-NULL");
+    if (!cam->width || !cam->height)
+        return IGXRT_OK;
+    const uint64_t pixels = (uint64_t)cam->width * cam->height;
+    if (pixels > 0x7fffffffu || cam->width > (1u << 24) || cam->height > (1u << 24))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "image too large");
+    if (((uintptr_t)dir_object % 16) || ((uintptr_t)uv_normal % 16))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "images must be 16-byte aligned");
+    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    igxrt_launch_params p;
+    st = resolve_params(ctx, ctx->params, p);
+    if (st != IGXRT_OK)
+        return st;
+    DeviceGuard guard(ctx->device);
+    if (!guard.ok())
+        return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    const bool host = flags & IGXRT_TRACE_HOST_MEMORY;
+    float4* d_do = reinterpret_cast<float4*>(dir_object);
+    float4* d_uv = reinterpret_cast<float4*>(uv_normal);
+    const size_t ib = pixels * sizeof(float4);
+    if (host) {
+        st = grow_stage(ctx, 2 * ((ib + 255) / 256 * 256));
+        if (st != IGXRT_OK)
+            return st;
+        d_do = static_cast<float4*>(ctx->d_stage);
+        d_uv = reinterpret_cast<float4*>(static_cast<char*>(ctx->d_stage) + (ib + 255) / 256 * 256);
+        // uv_normal is not written on a miss: carry the caller's contents
+        const cudaError_t e = cudaMemcpyAsync(d_uv, uv_normal, ib, cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "g-buffer upload");
+    } else if (!device_accessible(dir_object) || !device_accessible(uv_normal)) {
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
+    }
+    GbufferArgs a;
+    a.nodes = reinterpret_cast<const float4*>(scene->nodes[p.layout]);
+    a.prims = reinterpret_cast<const float4*>(scene->prims);
+    a.node_count = scene->node_count[p.layout];
+    a.tris = scene->tris;
+    a.cam = *cam;
+    a.inv_w = 1.0f / (float)cam->width;
+    a.inv_h = 1.0f / (float)cam->height;
+    a.tiles_x = (cam->width + 7) / 8;
+    a.tiles = a.tiles_x * ((cam->height + 3) / 4);
+    a.dir_object = d_do;
+    a.uv_normal = d_uv;
+    a.status = status_word(ctx);
+    a.sh_depth = p.stack_depth;
+    auto fn = p.layout == IGXRT_LAYOUT_BVH4 ? gbuffer_kernel<IGXRT_LAYOUT_BVH4> : gbuffer_kernel<IGXRT_LAYOUT_BVH2>;
+    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
+    int per_sm = 0;
+    cudaError_t e = allow_smem((const void*)fn, smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    if (e != cudaSuccess || per_sm < 1)
+        return e != cudaSuccess ? cuda_fail(ctx, e, "occupancy query")
+                                : fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "no resident CTA");
+    const uint64_t wpb = p.block_size / 32;
+    const uint32_t grid = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, (a.tiles + wpb - 1) / wpb));
+    fn<<<grid, p.block_size, smem, stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "g-buffer kernel launch");
+    if (host) {
+        e = cudaMemcpyAsync(dir_object, d_do, ib, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(uv_normal, d_uv, ib, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "g-buffer download");
+        return read_status(ctx);
+    }
+    return IGXRT_OK;
+}

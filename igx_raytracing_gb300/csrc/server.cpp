@@ -293,7 +293,7 @@ igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options*
     if (!s->opt.max_batch_requests)
         s->opt.max_batch_requests = 1024;
     if (!s->opt.streams)
-        s->opt.streams = 3;
+        s->opt.streams = 2;
     if (s->opt.max_batch_requests > 4096 || s->opt.streams > 16)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "max_batch_requests <= 4096, streams <= 16");
     igxrt_status st = resolve_params(ctx, ctx->params, s->params);

@@ -69,7 +69,7 @@ template <int LAYOUT, bool ANY, bool COUNT>
 __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
     extern __shared__ uint32_t smem[];
     TraversalStack st;
-    st.sh = smem + threadIdx.x;
+    st.sh = reinterpret_cast<uint2*>(smem) + threadIdx.x;
     st.stride = blockDim.x;
     st.sh_depth = a.sh_depth;
     st.sp = 0;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
             if (next < 0) {
                 occluded = process_leaf<ANY, COUNT>(a.prims, next, r, best, pf);
                 if (!occluded)
-                    next = st.sp == 0 ? kRefDone : st.pop();
+                    next = st.pop_live(best.tcull);
             }
             if (overflow)
                 atomicOr(a.status, kStatusStackOverflow);
@@ -164,9 +164,11 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     const igxrt_scene* s = req.scene;
     const bool count = req.node_fetches != nullptr;
     KernelFn fn = select_kernel(p.layout, req.mode == 1, count);
-    const size_t smem = (size_t)p.stack_depth * p.block_size * sizeof(uint32_t);
+    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    cudaError_t e = allow_smem((const void*)fn, smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "occupancy query");
     if (per_sm < 1)
@@ -211,9 +213,11 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
         return IGXRT_OK;
     const igxrt_scene* s = req.scene;
     KernelFn fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr);
-    const size_t smem = (size_t)p.stack_depth * p.block_size * sizeof(uint32_t);
+    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    cudaError_t e = allow_smem((const void*)fn, smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "occupancy query");
     if (per_sm < 1)

@@ -116,28 +116,42 @@ __device__ __forceinline__ bool tri_test(const RayState& r, const float4& v0, co
     return true;
 }
 
-// Traversal stack: the first `sh_depth` entries live in shared memory
-// (strided by the block size so a warp's pushes hit 32 banks), the rest in a
-// per-thread local array.
+constexpr int32_t kRefDone = 0x7fffffff;  // "stack empty": the traversal is over
+
+// Traversal stack of {child reference, entry distance of its box when it was
+// pushed}: the first `sh_depth` entries live in shared memory (strided by
+// the block size so a warp's accesses stay conflict-free), the rest in a
+// per-thread local array.  pop_live drops entries whose distance is beyond
+// the current cull limit without fetching them (their box test would fail
+// now), exactly as the host traversal does.
 struct TraversalStack {
-    uint32_t* sh;  // this thread's column of the block's shared stack
+    uint2* sh;  // this thread's column of the block's shared stack
     uint32_t stride;
     uint32_t sh_depth;
     uint32_t sp;
-    int32_t spill[kStackCapacityDevice];
+    uint2 spill[kStackCapacityDevice];
 
-    __device__ __forceinline__ void push(int32_t v) {
+    __device__ __forceinline__ void push(int32_t ref, float tnear) {
+        const uint2 e = make_uint2((uint32_t)ref, __float_as_uint(tnear));
         if (sp < sh_depth)
-            sh[sp * stride] = (uint32_t)v;
+            sh[sp * stride] = e;
         else
-            spill[sp - sh_depth] = v;
+            spill[sp - sh_depth] = e;
         ++sp;
     }
-    __device__ __forceinline__ int32_t pop() {
-        --sp;
-        return sp < sh_depth ? (int32_t)sh[sp * stride] : spill[sp - sh_depth];
+    __device__ __forceinline__ int32_t pop_live(float tcull) {
+        while (sp) {
+            --sp;
+            const uint2 e = sp < sh_depth ? sh[sp * stride] : spill[sp - sh_depth];
+            if (__uint_as_float(e.y) <= tcull)
+                return (int32_t)e.x;
+        }
+        return kRefDone;
     }
 };
+
+// Bytes of shared memory per stack entry and thread.
+constexpr uint32_t kStackEntryBytes = 8;
 
 // Closest-hit / any-hit leaf processing.  Returns true when an any-hit query
 // is decided (occluder found).
@@ -179,8 +193,6 @@ __device__ __forceinline__ void ldg256(const void* p, float4& lo, float4& hi) {
         : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w)
         : "l"(p));
 }
-
-constexpr int32_t kRefDone = 0x7fffffff;  // "stack empty": the traversal is over
 
 struct SlotKey {
     float tn;
@@ -230,7 +242,7 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
         m += h;
         SlotKey k3 = {h ? tn : INFINITY, ch.w, 3u};
         if (m == 0)
-            return st.sp == 0 ? kRefDone : st.pop();
+            return st.pop_live(best.tcull);
         // (tnear, slot) ascending; missed slots carry +inf and sort last (a
         // hit's tnear is at most the finite cull limit)
         order2(k0, k1);
@@ -243,11 +255,11 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
             return kRefDone;
         }
         if (m > 3)
-            st.push(k3.child);
+            st.push(k3.child, k3.tn);
         if (m > 2)
-            st.push(k2.child);
+            st.push(k2.child, k2.tn);
         if (m > 1)
-            st.push(k1.child);
+            st.push(k1.child, k1.tn);
         return k0.child;
     } else {
         const float4* n = nodes + 4 * (size_t)node;
@@ -264,14 +276,45 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
                 overflow = true;
                 return kRefDone;
             }
-            st.push(first1 ? c0 : c1);
+            st.push(first1 ? c0 : c1, first1 ? tn0 : tn1);
             return first1 ? c1 : c0;
         }
         if (h0)
             return c0;
         if (h1)
             return c1;
-        return st.sp == 0 ? kRefDone : st.pop();
+        return st.pop_live(best.tcull);
+    }
+}
+
+// Whole traversal of one ray by one thread (no refill), in the same order as
+// the persistent kernels.  ANY: returns true at the first occluder.
+// Otherwise `best` ends as the closest hit.
+template <int LAYOUT, bool ANY>
+__device__ __forceinline__ bool trace_single(const float4* __restrict__ nodes,
+                                             const float4* __restrict__ prims, uint32_t node_count,
+                                             const RayState& r, BestHit& best, TraversalStack& st,
+                                             bool& overflow) {
+    best.t = r.tmax_eff;
+    best.u = 0.f;
+    best.v = 0.f;
+    best.prim = 0;
+    best.tcull = cull_limit(best.t);
+    if (!node_count)
+        return false;
+    st.sp = 0;
+    uint32_t unused = 0;
+    int32_t next = 0;
+    for (;;) {
+        while (next >= 0 && next != kRefDone)
+            next = visit_node<LAYOUT, false>(nodes, next, r, best, st, overflow, unused);
+        if (next == kRefDone)
+            return false;
+        if (process_leaf<ANY, false>(prims, next, r, best, unused))
+            return true;
+        next = st.pop_live(best.tcull);
+        if (next == kRefDone)
+            return false;
     }
 }
 

@@ -145,6 +145,30 @@ def pinhole_rays(width: int, height: int, eye, target, up=(0.0, 0.0, 1.0), vfov_
     return r
 
 
+def camera_record(width: int, height: int, eye, target, up=(0.0, 0.0, 1.0), vfov_deg: float = 60.0,
+                  jitter=(0.5, 0.5)) -> np.ndarray:
+    """igxrt_camera for the G-buffer pass: the same pinhole corners as
+    pinhole_rays (p0 top left, p1 top right, p2 bottom left at distance 1)."""
+    from ._capi import CAMERA_DTYPE
+
+    eye = np.asarray(eye, dtype=np.float64)
+    fwd = np.asarray(target, dtype=np.float64) - eye
+    fwd /= np.linalg.norm(fwd)
+    right = np.cross(fwd, np.asarray(up, dtype=np.float64))
+    right /= np.linalg.norm(right)
+    upv = np.cross(right, fwd)
+    h = math.tan(math.radians(vfov_deg) * 0.5)
+    aspect = width / height
+    c = np.zeros(1, dtype=CAMERA_DTYPE)
+    c["eye"] = eye
+    c["p0"] = eye + fwd - aspect * h * right + h * upv
+    c["p1"] = eye + fwd + aspect * h * right + h * upv
+    c["p2"] = eye + fwd - aspect * h * right - h * upv
+    c["width"], c["height"] = width, height
+    c["jitter_x"], c["jitter_y"] = jitter
+    return c
+
+
 def sphere_dirs(n: int, rng: np.random.Generator) -> np.ndarray:
     z = rng.uniform(-1.0, 1.0, n)
     phi = rng.uniform(0.0, 2 * np.pi, n)

@@ -354,7 +354,7 @@ typedef struct igxrt_server_options {
                                     buffers of admitted requests; 0 = 24 GiB */
     uint32_t max_batch_rays;     /* rays coalesced into one launch, 0 = 4M */
     uint32_t max_batch_requests; /* requests per launch, 0 = 1024 (at most 4096) */
-    uint32_t streams;            /* batches in flight at once, 0 = 3 */
+    uint32_t streams;            /* batches in flight at once, 0 = 2 */
     uint32_t reserved[3];
 } igxrt_server_options;
 
@@ -410,6 +410,60 @@ igxrt_status igxrt_server_wait(igxrt_server* server, uint64_t ticket, double tim
 igxrt_status igxrt_server_get_stats(igxrt_server* server, igxrt_server_stats* stats);
 /* Finishes all queued work, then stops the scheduler and frees its memory. */
 igxrt_status igxrt_server_destroy(igxrt_server* server);
+
+/*
+ * Fused shadow pass: nv_all.shadow.comp (res/shaders/nv_all.shadow.comp:50-142)
+ * as one kernel.  One any-hit ray per pixel and sample; the results are packed
+ * into the 32-bit ballot words the lighting pass reads (light_rt.glsl:17-28):
+ * a word per 16x2 pixel tile and sample at indexToLight(loc, res, sample)
+ * (light.glsl:221-229) = tile.x + tile.y*tiles_x + sample*tiles_x*tiles_y with
+ * tiles_x = ceil(width/16), tiles_y = ceil(height/2); pixel (x, y) owns bit
+ * (x & 15) | ((y & 1) << 4).
+ *   rays:   width*height*samples rays, ray (sample*height + y)*width + x;
+ *           its tmax is the shadow distance (traceOcclusion's maxDist).
+ *   object: width*height primary objects (dirObject.w of raygen.comp); a
+ *           pixel whose object is IGXRT_NO_RAY_HIT casts no ray and its bit is
+ *           0; otherwise its rays exclude that object (prevHit).
+ *   mask:   tiles_x*tiles_y*samples words, every one written (the shader's
+ *           non-DEBUG build leaves all-empty tiles unwritten; here they are 0).
+ */
+igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_scene* scene,
+                                     const igxrt_ray* rays, const uint32_t* object,
+                                     uint32_t width, uint32_t height, uint32_t samples,
+                                     uint32_t* mask, uint32_t flags, void* stream);
+
+/*
+ * Camera of the reference's default projection (res/shaders/camera.glsl:14-42):
+ * the eye and three corners of the image plane, p0 top left, p1 top right,
+ * p2 bottom left.  jitter is added to the pixel index before the division by
+ * the resolution (the reference adds rand(loc + seed); 0.5 = pixel centres).
+ */
+typedef struct igxrt_camera {
+    float eye[3];
+    uint32_t width;
+    float p0[3];
+    uint32_t height;
+    float p1[3];
+    float jitter_x;
+    float p2[3];
+    float jitter_y;
+} igxrt_camera;
+
+/*
+ * Fused primary pass: raygen.comp (res/shaders/raygen.comp:16-52) with the
+ * default projection as one kernel.  For pixel (x, y), y = loc.y:
+ *   c = ((x, y) + jitter) * (1/width, 1/height), c.y = 1 - c.y
+ *   dir = normalize(p0 + c.x*(p1 - p0) + c.y*(p2 - p0) - eye)   (camera.glsl:72-87, 113-116)
+ *   hit = traceGeometry((eye, dir), noRayHit)
+ * and the shader's two rgba32f images, row-major (pixel y*width + x):
+ *   dir_object = {dir*t, bits(object)} on a hit, {dir, bits(noRayHit)} on a miss (:39-44);
+ *   uv_normal  = {u, v, bits(encodeNormal(objectNormal))} on a hit, not written on a miss (:46-51),
+ * with objectNormal = interpolate(decodeSpheremap(n0), decodeSpheremap(n1),
+ * decodeSpheremap(n2), uv) of the hit triangle (trace.glsl:48-57).
+ */
+igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scene* scene,
+                                 const igxrt_camera* camera, float* dir_object, float* uv_normal,
+                                 uint32_t flags, void* stream);
 
 /* Copies `count` device hits to host memory and waits for them. */
 igxrt_status igxrt_fetch_hits(igxrt_context* ctx, const igxrt_hit* device_hits,

@@ -62,6 +62,33 @@ int orc_bvh_trace(uint32_t layout, const void* nodes, uint64_t node_count,
                   uint32_t mode, igxrt_hit* out_hits, uint32_t* out_occluded,
                   uint32_t* node_fetches, uint32_t* prim_fetches, int threads);
 
+/*
+ * The shadow pass of res/shaders/nv_all.shadow.comp:50-142 on the NVIDIA
+ * subgroup layout: per pixel (x, y) and sample s with object != noRayHit,
+ * traceOcclusion(ray, ray.tmax, object) by brute force; the results are
+ * ballot-packed into words indexToLight(loc, res, s, (4,1), (15,1))
+ * (res/shaders/light.glsl:221-229), bit (x & 15) | ((y & 1) << 4).  Every
+ * word is written (0 where no pixel is occluded).  flags as for
+ * orc_trace_occlusion, per ray (may be NULL).
+ */
+void orc_shadow_mask(const igxrt_triangle* tris, uint32_t ntri, const igxrt_ray* rays,
+                     const uint32_t* object, uint32_t width, uint32_t height, uint32_t samples,
+                     uint32_t* mask, uint32_t* flags, int threads);
+
+/*
+ * The primary pass of res/shaders/raygen.comp:16-52 (default projection):
+ * calculateScreen's ray per pixel (camera.glsl:72-87, 113-116), brute-force
+ * traceGeometry, and the shader's two rgba32f outputs (dir_object, uv_normal:
+ * width*height*4 floats each, row-major; uv_normal untouched on a miss).
+ * flags per pixel as for orc_trace_geometry (may be NULL).
+ */
+void orc_gbuffer(const igxrt_triangle* tris, uint32_t ntri, const igxrt_camera* cam,
+                 float* dir_object, float* uv_normal, uint32_t* flags, int threads);
+
+/* decodeSpheremap (primitive.glsl:95-104) and encodeNormal (:85-88). */
+void orc_decode_spheremap(uint32_t n, float out[3]);
+void orc_encode_normal(const float n[3], uint32_t out[2]);
+
 /* Number of hardware threads the oracle uses for threads <= 0. */
 int orc_hardware_threads(void);
 

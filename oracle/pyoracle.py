@@ -60,6 +60,14 @@ def lib() -> C.CDLL:
         h.orc_reintersect_f64.restype = i32
         h.orc_bvh_trace.argtypes = [u32, vp, u64, vp, u64, vp, vp, u32, u32, vp, vp, vp, vp, i32]
         h.orc_bvh_trace.restype = i32
+        h.orc_shadow_mask.argtypes = [vp, u32, vp, vp, u32, u32, u32, vp, vp, i32]
+        h.orc_shadow_mask.restype = None
+        h.orc_gbuffer.argtypes = [vp, u32, vp, vp, vp, vp, i32]
+        h.orc_gbuffer.restype = None
+        h.orc_decode_spheremap.argtypes = [u32, vp]
+        h.orc_decode_spheremap.restype = None
+        h.orc_encode_normal.argtypes = [vp, vp]
+        h.orc_encode_normal.restype = None
         h.orc_hardware_threads.argtypes = []
         h.orc_hardware_threads.restype = i32
         _lib = h
@@ -128,6 +136,72 @@ def trace_occlusion(tris: np.ndarray, rays: np.ndarray, prev=None, threads: int 
         lib().orc_trace_occlusion(_ptr(tris), len(tris), _ptr(rays), _ptr(p), n, _ptr(out),
                                   _ptr(flags), threads)
     return out, flags
+
+
+def shadow_mask(tris, rays, object_, width: int, height: int, samples: int, threads: int = 0):
+    """The reference's shadow pass (brute force) packed into ballot words."""
+    tris = np.ascontiguousarray(tris)
+    rays = np.ascontiguousarray(rays)
+    obj = np.ascontiguousarray(object_, dtype=np.uint32)
+    assert len(rays) == width * height * samples and len(obj) == width * height
+    words = ((width + 15) // 16) * ((height + 1) // 2) * samples
+    mask = np.zeros(words, dtype=np.uint32)
+    flags = np.zeros(len(rays), dtype=np.uint32)
+    lib().orc_shadow_mask(_ptr(tris), len(tris), _ptr(rays), _ptr(obj), width, height, samples,
+                          _ptr(mask), _ptr(flags), threads)
+    return mask, flags
+
+
+CAMERA_DTYPE = np.dtype([("eye", "<f4", (3,)), ("width", "<u4"), ("p0", "<f4", (3,)),
+                         ("height", "<u4"), ("p1", "<f4", (3,)), ("jitter_x", "<f4"),
+                         ("p2", "<f4", (3,)), ("jitter_y", "<f4")])
+
+
+def gbuffer(tris, camera: np.ndarray, threads: int = 0, uv_fill: float = 0.0):
+    """The reference's primary pass: (dir_object, uv_normal, flags), images
+    (height, width, 4) float32; uv_normal keeps uv_fill where rays miss."""
+    tris = np.ascontiguousarray(tris)
+    cam = np.ascontiguousarray(camera, dtype=CAMERA_DTYPE).reshape(1)
+    w, h = int(cam["width"][0]), int(cam["height"][0])
+    do = np.zeros((h, w, 4), dtype=np.float32)
+    uv = np.full((h, w, 4), uv_fill, dtype=np.float32)
+    flags = np.zeros(w * h, dtype=np.uint32)
+    lib().orc_gbuffer(_ptr(tris), len(tris), _ptr(cam), _ptr(do), _ptr(uv), _ptr(flags), threads)
+    return do, uv, flags
+
+
+def decode_spheremap(packed) -> np.ndarray:
+    out = np.zeros((len(packed), 3), dtype=np.float32)
+    tmp = np.zeros(3, dtype=np.float32)
+    for i, p in enumerate(np.asarray(packed, dtype=np.uint32)):
+        lib().orc_decode_spheremap(int(p), _ptr(tmp))
+        out[i] = tmp
+    return out
+
+
+def encode_normal(normals) -> np.ndarray:
+    n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros((len(n), 2), dtype=np.uint32)
+    tmp = np.zeros(2, dtype=np.uint32)
+    for i in range(len(n)):
+        row = np.ascontiguousarray(n[i])
+        lib().orc_encode_normal(_ptr(row), _ptr(tmp))
+        out[i] = tmp
+    return out
+
+
+def ref_decode_spheremap(packed) -> np.ndarray:
+    p = np.ascontiguousarray(packed, dtype=np.uint32)
+    out = np.zeros((len(p), 3), dtype=np.float32)
+    ref_lib().igxref_decode_spheremap(_ptr(p), len(p), _ptr(out))
+    return out
+
+
+def ref_encode_normal(normals) -> np.ndarray:
+    n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros((len(n), 2), dtype=np.uint32)
+    ref_lib().igxref_encode_normal(_ptr(n), len(n), _ptr(out))
+    return out
 
 
 def reintersect_f64(ray: np.ndarray, tri: np.ndarray):

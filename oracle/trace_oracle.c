@@ -263,6 +263,188 @@ void orc_trace_occlusion(const igxrt_triangle* tris, uint32_t ntri, const igxrt_
     run_parallel(brute_any_chunk, &c, nrays, 64, threads);
 }
 
+/* unpackHalf2x16 component: exact binary16 -> binary32. */
+static float half_to_float(uint32_t h) {
+    const uint32_t sign = (h >> 15) & 1u, ex = (h >> 10) & 31u, man = h & 1023u;
+    float mag;
+    if (ex == 0) {
+        mag = (float)man * 0x1p-24f;
+    } else if (ex == 31) {
+        mag = man ? NAN : INFINITY;
+    } else {
+        const uint32_t bits = ((ex + 112u) << 23) | (man << 13);
+        memcpy(&mag, &bits, 4);
+    }
+    return sign ? -mag : mag;
+}
+
+/* decodeSpheremap, primitive.glsl:95-104. */
+void orc_decode_spheremap(uint32_t n, float out[3]) {
+    float x = half_to_float(n & 0xffffu), y = half_to_float(n >> 16);
+    const v3 a = {x, y, 1.0f}, b = {-x, -y, 1.0f}; /* vec3(nn, 1), -vec3(nn, -1) */
+    const float l = dot(a, b);
+    const float s = sqrtf(l);
+    x = x * s; /* nn *= sqrt(l) */
+    y = y * s;
+    out[0] = x * 2 + 0.0f; /* vec3(nn, l) * 2 + vec3(0, 0, -1) */
+    out[1] = y * 2 + 0.0f;
+    out[2] = l * 2 + -1.0f;
+}
+
+/* float -> uint conversion with the GPU's rule for the out-of-range
+ * values GLSL leaves undefined: NaN and negatives give 0. */
+static uint32_t f2u(float f) {
+    if (!(f > 0.0f))
+        return 0u;
+    if (f >= 4294967296.0f)
+        return 0xffffffffu;
+    return (uint32_t)f;
+}
+
+/* encodeNormal, primitive.glsl:85-88. */
+void orc_encode_normal(const float n[3], uint32_t out[2]) {
+    const v3 v = {n[0], n[1], n[2]};
+    const float len = sqrtf(dot(v, v)); /* normalize(n) = n / length(n) */
+    const uint32_t hx = f2u((n[0] / len * 0.5f + 0.5f) * 65535.0f);
+    const uint32_t hy = f2u((n[1] / len * 0.5f + 0.5f) * 65535.0f);
+    const uint32_t hz = f2u((n[2] / len * 0.5f + 0.5f) * 65535.0f);
+    out[0] = (hx << 16) | hy;
+    out[1] = hz;
+}
+
+typedef struct {
+    const igxrt_triangle* tris;
+    uint32_t ntri;
+    const igxrt_camera* cam;
+    float inv_w, inv_h;
+    float* dir_object;
+    float* uv_normal;
+    uint32_t* flags;
+} gbuffer_ctx;
+
+static void gbuffer_chunk(void* p, uint32_t b, uint32_t e) {
+    gbuffer_ctx* g = (gbuffer_ctx*)p;
+    const igxrt_camera* c = g->cam;
+    for (uint32_t i = b; i < e; ++i) {
+        const uint32_t x = i % c->width, y = i / c->width;
+        /* calculatePrimary (camera.glsl:115-116) and calculateScreen (:72-87) */
+        const float cx = ((float)x + c->jitter_x) * g->inv_w;
+        const float cy = 1 - ((float)y + c->jitter_y) * g->inv_h;
+        float d[3];
+        for (int k = 0; k < 3; ++k) {
+            const float right = c->p1[k] - c->p0[k], up = c->p2[k] - c->p0[k];
+            const float pos = c->p0[k] + cx * right + cy * up;
+            d[k] = pos - c->eye[k];
+        }
+        const v3 dv = {d[0], d[1], d[2]};
+        const float len = sqrtf(dot(dv, dv));
+        igxrt_ray ray;
+        for (int k = 0; k < 3; ++k) {
+            ray.org[k] = c->eye[k];
+            ray.dir[k] = d[k] / len;
+        }
+        ray.tmin = 0.0f;
+        ray.tmax = IGXRT_NO_HIT;
+        igxrt_hit h;
+        uint32_t f = 0;
+        trace_geometry_one(g->tris, g->ntri, &ray, IGXRT_NO_RAY_HIT, &h, &f);
+        if (g->flags)
+            g->flags[i] = f;
+        float* dob = g->dir_object + 4 * (size_t)i;
+        if (h.prim != IGXRT_NO_RAY_HIT) {
+            /* raygen.comp:39: vec4(hit.rayDir * hit.hitT, uintBitsToFloat(hit.object)) */
+            for (int k = 0; k < 3; ++k)
+                dob[k] = ray.dir[k] * h.t;
+            memcpy(&dob[3], &h.prim, 4);
+            /* trace.glsl:50-57, raygen.comp:46-51 */
+            const igxrt_triangle* t = &g->tris[h.prim];
+            float n0[3], n1[3], n2[3], n[3];
+            orc_decode_spheremap(t->n0, n0);
+            orc_decode_spheremap(t->n1, n1);
+            orc_decode_spheremap(t->n2, n2);
+            const float bw = 1 - h.u - h.v; /* interpolate, primitive.glsl:146-151 */
+            for (int k = 0; k < 3; ++k)
+                n[k] = h.u * n1[k] + h.v * n2[k] + bw * n0[k];
+            uint32_t enc[2];
+            orc_encode_normal(n, enc);
+            float* uvn = g->uv_normal + 4 * (size_t)i;
+            uvn[0] = h.u;
+            uvn[1] = h.v;
+            memcpy(&uvn[2], enc, 8);
+        } else {
+            /* raygen.comp:40-41: vec4(hit.rayDir, uintBitsToFloat(noRayHit)) */
+            const uint32_t none = IGXRT_NO_RAY_HIT;
+            for (int k = 0; k < 3; ++k)
+                dob[k] = ray.dir[k];
+            memcpy(&dob[3], &none, 4);
+        }
+    }
+}
+
+void orc_gbuffer(const igxrt_triangle* tris, uint32_t ntri, const igxrt_camera* cam,
+                 float* dir_object, float* uv_normal, uint32_t* flags, int threads) {
+    gbuffer_ctx g = {tris, ntri, cam, 1.0f / (float)cam->width, 1.0f / (float)cam->height,
+                     dir_object, uv_normal, flags};
+    run_parallel(gbuffer_chunk, &g, cam->width * cam->height, 64, threads);
+}
+
+/* indexToLight, res/shaders/light.glsl:221-229. */
+static uint32_t index_to_light(uint32_t lx, uint32_t ly, uint32_t rx, uint32_t ry, uint32_t light,
+                               uint32_t shx, uint32_t shy, uint32_t mx, uint32_t my) {
+    const uint32_t tile_x = lx >> shx, tile_y = ly >> shy;
+    uint32_t tiles_x = rx >> shx, tiles_y = ry >> shy;
+    tiles_x += (rx & mx) != 0; /* ceil(res / threads) */
+    tiles_y += (ry & my) != 0;
+    return tile_x + tile_y * tiles_x + light * tiles_y * tiles_x;
+}
+
+typedef struct {
+    const igxrt_triangle* tris;
+    uint32_t ntri;
+    const igxrt_ray* rays;
+    const uint32_t* object;
+    uint32_t w, h;
+    uint32_t* occ;
+    uint32_t* flags;
+} shadow_ctx;
+
+static void shadow_chunk(void* p, uint32_t b, uint32_t e) {
+    shadow_ctx* c = (shadow_ctx*)p;
+    for (uint32_t i = b; i < e; ++i) {
+        const uint32_t pix = i % (c->w * c->h);
+        const uint32_t obj = c->object[pix];
+        uint32_t f = 0;
+        c->occ[i] = 0;
+        if (obj != IGXRT_NO_RAY_HIT) /* nv_all.shadow.comp:108 */
+            trace_occlusion_one(c->tris, c->ntri, &c->rays[i], obj, &c->occ[i], &f);
+        if (c->flags)
+            c->flags[i] = f;
+    }
+}
+
+void orc_shadow_mask(const igxrt_triangle* tris, uint32_t ntri, const igxrt_ray* rays,
+                     const uint32_t* object, uint32_t width, uint32_t height, uint32_t samples,
+                     uint32_t* mask, uint32_t* flags, int threads) {
+    const uint32_t n = width * height * samples;
+    uint32_t* occ = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
+    shadow_ctx c = {tris, ntri, rays, object, width, height, occ, flags};
+    run_parallel(shadow_chunk, &c, n, 64, threads);
+    const uint32_t tiles_x = (width + 15) / 16, tiles_y = (height + 1) / 2;
+    memset(mask, 0, sizeof(uint32_t) * (size_t)tiles_x * tiles_y * samples);
+    for (uint32_t s = 0; s < samples; ++s)
+        for (uint32_t y = 0; y < height; ++y)
+            for (uint32_t x = 0; x < width; ++x) {
+                if (!occ[((size_t)s * height + y) * width + x])
+                    continue;
+                /* ballotARB(hit) over the 16x2 subgroup, stored by lane 0
+                 * (nv_all.shadow.comp:128-138) */
+                const uint32_t word = index_to_light(x, y, width, height, s, 4, 1, 15, 1);
+                const uint32_t lane = (x & 15) | ((y & 1) << 4);
+                mask[word] |= 1u << lane;
+            }
+    free(occ);
+}
+
 int orc_reintersect_f64(const igxrt_ray* ray, const igxrt_triangle* tri, double* t_out,
                         double* u_out, double* v_out) {
     double o[3], d[3], p0[3], e1[3], e2[3];
@@ -389,11 +571,31 @@ static inline int leaf_record(const rayprep* r, const igxrt_prim_record* rec, be
     return 0;
 }
 
+/* Traversal stack entry: a pushed child and the entry distance its box had
+ * when it was pushed.  A popped entry whose distance is beyond the current
+ * cull limit is dropped without fetching: its box test would now fail. */
+typedef struct {
+    int32_t ref;
+    float tnear;
+} stack_entry;
+
+/* Pops the next live entry into *next; returns 0 when the stack runs out. */
+static inline int pop_live(const stack_entry* stack, int* sp, float tcull, int32_t* next) {
+    while (*sp > 0) {
+        const stack_entry e = stack[--*sp];
+        if (e.tnear <= tcull) {
+            *next = e.ref;
+            return 1;
+        }
+    }
+    return 0;
+}
+
 static int bvh2_trace_one(const igxrt_bvh2_node* nodes, uint64_t nn,
                           const igxrt_prim_record* prims, uint64_t np, const rayprep* r,
                           int anyhit, best_hit* b, uint32_t* occluded, uint32_t* nf,
                           uint32_t* pf) {
-    int32_t stack[ORC_STACK];
+    stack_entry stack[ORC_STACK];
     int sp = 0;
     *occluded = 0;
     if (nn == 0)
@@ -414,16 +616,16 @@ static int bvh2_trace_one(const igxrt_bvh2_node* nodes, uint64_t nn,
                 const int first = tn1 < tn0 ? 1 : 0;
                 if (sp >= ORC_STACK)
                     return -1;
-                stack[sp++] = n->child[1 - first];
+                stack[sp].ref = n->child[1 - first];
+                stack[sp].tnear = first ? tn0 : tn1;
+                ++sp;
                 next = n->child[first];
             } else if (h0) {
                 next = n->child[0];
             } else if (h1) {
                 next = n->child[1];
-            } else {
-                if (sp == 0)
-                    break;
-                next = stack[--sp];
+            } else if (!pop_live(stack, &sp, b->tcull, &next)) {
+                break;
             }
         } else {
             uint64_t i = (uint64_t)(uint32_t)~next;
@@ -440,9 +642,8 @@ static int bvh2_trace_one(const igxrt_bvh2_node* nodes, uint64_t nn,
                     break;
                 ++i;
             }
-            if (sp == 0)
+            if (!pop_live(stack, &sp, b->tcull, &next))
                 break;
-            next = stack[--sp];
         }
     }
     return 0;
@@ -452,7 +653,7 @@ static int bvh4_trace_one(const igxrt_bvh4_node* nodes, uint64_t nn,
                           const igxrt_prim_record* prims, uint64_t np, const rayprep* r,
                           int anyhit, best_hit* b, uint32_t* occluded, uint32_t* nf,
                           uint32_t* pf) {
-    int32_t stack[ORC_STACK];
+    stack_entry stack[ORC_STACK];
     int sp = 0;
     *occluded = 0;
     if (nn == 0)
@@ -483,14 +684,16 @@ static int bvh4_trace_one(const igxrt_bvh4_node* nodes, uint64_t nn,
                 }
             }
             if (m == 0) {
-                if (sp == 0)
+                if (!pop_live(stack, &sp, b->tcull, &next))
                     break;
-                next = stack[--sp];
             } else {
                 if (sp + m - 1 > ORC_STACK)
                     return -1;
-                for (int j = m - 1; j >= 1; --j)
-                    stack[sp++] = n->child[slot[j]];
+                for (int j = m - 1; j >= 1; --j) {
+                    stack[sp].ref = n->child[slot[j]];
+                    stack[sp].tnear = tn[j];
+                    ++sp;
+                }
                 next = n->child[slot[0]];
             }
         } else {
@@ -508,9 +711,8 @@ static int bvh4_trace_one(const igxrt_bvh4_node* nodes, uint64_t nn,
                     break;
                 ++i;
             }
-            if (sp == 0)
+            if (!pop_live(stack, &sp, b->tcull, &next))
                 break;
-            next = stack[--sp];
         }
     }
     return 0;

@@ -166,6 +166,31 @@ def main() -> None:
                         object_normal=h["objectNormal"])
     print(f"niels_mixed: {len(r)} rays, {int((h['hitT'] < NO_HIT).sum())} hits")
 
+    # 5. packed vertex normals: decodeSpheremap, interpolate and encodeNormal
+    rng2 = np.random.default_rng(scenes.seed_for(9, 1))
+
+    def packed(n):
+        rad = np.sqrt(rng2.uniform(0, 1, n)) * 0.999
+        ang = rng2.uniform(0, 2 * np.pi, n)
+        hx = (rad * np.cos(ang)).astype(np.float16).view(np.uint16).astype(np.uint32)
+        hy = (rad * np.sin(ang)).astype(np.float16).view(np.uint16).astype(np.uint32)
+        return (hx | (hy << 16)).astype(np.uint32)
+
+    nt = scenes.random_triangles(1024, scenes.seed_for(3, 79), mu=math.log(0.06))
+    for f in ("n0", "n1", "n2"):
+        nt[f] = packed(len(nt))
+    nr = scenes.incoherent_rays(4096, scenes.seed_for(3, 80), tmax=float(NO_HIT))
+    h = pyoracle.ref_trace_geometry(nt, rays6(nr))
+    miss = h["hitT"] == NO_HIT
+    dec_in = packed(2048)
+    enc_in = rng2.normal(size=(2048, 3)).astype(np.float32) * rng2.uniform(0.2, 3.0, (2048, 1)).astype(np.float32)
+    np.savez_compressed(
+        os.path.join(HERE, "normals.npz"), tris=nt, rays=nr, hit_t=h["hitT"], hit_u=h["uv"][:, 0],
+        hit_v=h["uv"][:, 1], hit_prim=np.where(miss, np.uint32(0xFFFFFFFF), h["object"]).astype(np.uint32),
+        object_normal=h["objectNormal"], dec_in=dec_in, dec_out=pyoracle.ref_decode_spheremap(dec_in),
+        enc_in=enc_in, enc_out=pyoracle.ref_encode_normal(enc_in))
+    print(f"normals: {len(nr)} rays, {int((~miss).sum())} hits")
+
 
 if __name__ == "__main__":
     main()

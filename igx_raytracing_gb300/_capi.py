@@ -66,7 +66,8 @@ class BvhInfo(C.Structure):
                 ("bvh4_nodes", C.c_uint32), ("leaf_count", C.c_uint32), ("max_depth", C.c_uint32),
                 ("max_leaf_size", C.c_uint32), ("sah_cost", C.c_float), ("bounds", C.c_float * 6),
                 ("pad_abs", C.c_float), ("max_stack", C.c_uint32 * LAYOUT_COUNT),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("sphere_count", C.c_uint32),
+                ("cube_count", C.c_uint32), ("plane_count", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class LaunchParams(C.Structure):
@@ -214,4 +215,21 @@ assert CAMERA_DTYPE.itemsize == 64
 
 PROTOTYPES += [
     ("igxrt_trace_gbuffer", _st, [_vp, _vp, _vp, _vp, _vp, _u32, _vp]),
+]
+
+# igxrt_cube (24 bytes) and igxrt_scene_desc
+CUBE_DTYPE = np.dtype([("xy0", "<f4", (2,)), ("z0_x1", "<f4", (2,)), ("yz1", "<f4", (2,))])
+assert CUBE_DTYPE.itemsize == 24
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("triangles", C.c_void_p), ("triangle_count", C.c_uint32),
+                ("sphere_count", C.c_uint32), ("spheres", C.c_void_p), ("cubes", C.c_void_p),
+                ("cube_count", C.c_uint32), ("plane_count", C.c_uint32), ("planes", C.c_void_p)]
+
+
+PROTOTYPES += [
+    ("igxrt_bvh_build_mixed", _st, [C.POINTER(SceneDesc), C.POINTER(BuildOptions), C.POINTER(_vp)]),
+    ("igxrt_scene_create_mixed", _st, [_vp, C.POINTER(SceneDesc), C.POINTER(BuildOptions),
+                                       C.POINTER(_vp)]),
 ]

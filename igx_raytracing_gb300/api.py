@@ -84,7 +84,30 @@ def _info_dict(info: BvhInfo) -> dict:
         "max_depth": info.max_depth, "max_leaf_size": info.max_leaf_size,
         "sah_cost": info.sah_cost, "bounds": list(info.bounds), "pad_abs": info.pad_abs,
         "max_stack": list(info.max_stack), "device_bytes": info.device_bytes,
+        "sphere_count": info.sphere_count, "cube_count": info.cube_count,
+        "plane_count": info.plane_count,
     }
+
+
+def scene_desc(triangles=None, spheres=None, cubes=None, planes=None):
+    """igxrt_scene_desc over host arrays; returns (desc, arrays kept alive).
+    spheres / planes: (N, 4) float32; cubes: CUBE_DTYPE or (N, 6) float32."""
+    t = None if triangles is None else as_triangles(triangles)
+    s = None if spheres is None else np.ascontiguousarray(spheres, dtype=np.float32).reshape(-1, 4)
+    c = None
+    if cubes is not None:
+        c = np.asarray(cubes)
+        c = (np.ascontiguousarray(c) if c.dtype == _capi.CUBE_DTYPE
+             else np.ascontiguousarray(c, dtype=np.float32).reshape(-1, 6).view(_capi.CUBE_DTYPE).reshape(-1))
+    p = None if planes is None else np.ascontiguousarray(planes, dtype=np.float32).reshape(-1, 4)
+    d = _capi.SceneDesc()
+    for field, arr in (("triangles", t), ("spheres", s), ("cubes", c), ("planes", p)):
+        setattr(d, field, arr.ctypes.data if arr is not None and len(arr) else None)
+    d.triangle_count = 0 if t is None else len(t)
+    d.sphere_count = 0 if s is None else len(s)
+    d.cube_count = 0 if c is None else len(c)
+    d.plane_count = 0 if p is None else len(p)
+    return d, (t, s, c, p)
 
 
 class BVH:
@@ -100,6 +123,15 @@ class BVH:
         o = _build_options(**opts)
         check(lib().igxrt_bvh_build(tris.ctypes.data if len(tris) else None, len(tris),
                                     C.byref(o), C.byref(h)), what="igxrt_bvh_build")
+        return cls(h.value)
+
+    @classmethod
+    def build_mixed(cls, triangles=None, spheres=None, cubes=None, planes=None, **opts) -> "BVH":
+        d, keep = scene_desc(triangles, spheres, cubes, planes)
+        h = C.c_void_p()
+        o = _build_options(**opts)
+        check(lib().igxrt_bvh_build_mixed(C.byref(d), C.byref(o), C.byref(h)),
+              what="igxrt_bvh_build_mixed")
         return cls(h.value)
 
     @classmethod
@@ -252,6 +284,17 @@ class Context:
                                        len(tris), C.byref(o), C.byref(h)), self._h,
               "igxrt_scene_create")
         return Scene(self, h.value, len(tris))
+
+    def create_scene_mixed(self, triangles=None, spheres=None, cubes=None, planes=None,
+                           **opts) -> Scene:
+        """A scene of all the reference's primitive types (scene.glsl:22-39);
+        object ids: triangles, then spheres, cubes, planes."""
+        d, keep = scene_desc(triangles, spheres, cubes, planes)
+        h = C.c_void_p()
+        o = _build_options(**opts)
+        check(lib().igxrt_scene_create_mixed(self._h, C.byref(d), C.byref(o), C.byref(h)),
+              self._h, "igxrt_scene_create_mixed")
+        return Scene(self, h.value, d.triangle_count)
 
     # -- queries -----------------------------------------------------------
     @staticmethod

@@ -169,6 +169,9 @@ igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: scene is NULL", i));
         if (it.scene->device != ctx->device)
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: scene on another device", i));
+        if (it.scene->mixed)
+            return fail(ctx, IGXRT_ERROR_UNSUPPORTED,
+                        format("item %u: batches take triangle-only scenes", i));
         if (it.mode > 1)
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: unknown mode %u", i, it.mode));
         if (it.count && (!it.rays || !it.out))

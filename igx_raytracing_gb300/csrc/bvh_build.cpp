@@ -77,7 +77,7 @@ struct BNode {
 };
 
 struct Builder {
-    const igxrt_triangle* tris = nullptr;
+    const igxrt_scene_desc* d = nullptr;  // primitives: triangles, spheres, cubes
     uint32_t n = 0;
     uint32_t max_leaf = 8;
     uint32_t bins = 32;
@@ -262,18 +262,36 @@ struct Layout {
         const BNode& nd = b.nodes[id];
         const uint32_t first = (uint32_t)out.prims.size();
         leaf_rec[id] = first;
+        const uint32_t nt = b.d->triangle_count, ns = b.d->sphere_count;
         for (uint32_t k = 0; k < nd.count; ++k) {
-            const uint32_t t = b.refs[nd.first + k];
-            const igxrt_triangle& tri = b.tris[t];
-            igxrt_prim_record rec;
-            for (int a = 0; a < 3; ++a) {
-                rec.p0[a] = tri.p0[a];
-                rec.e1[a] = tri.p1[a] - tri.p0[a];
-                rec.e2[a] = tri.p2[a] - tri.p0[a];
+            const uint32_t t = b.refs[nd.first + k];  // global object id
+            igxrt_prim_record rec{};
+            if (t < nt) {
+                const igxrt_triangle& tri = b.d->triangles[t];
+                for (int a = 0; a < 3; ++a) {
+                    rec.p0[a] = tri.p0[a];
+                    rec.e1[a] = tri.p1[a] - tri.p0[a];
+                    rec.e2[a] = tri.p2[a] - tri.p0[a];
+                }
+                rec.pad = kPrimTriangle;
+            } else if (t < nt + ns) {
+                const float* s = b.d->spheres + 4 * (size_t)(t - nt);
+                for (int a = 0; a < 3; ++a)
+                    rec.p0[a] = s[a];
+                rec.e1[0] = s[3];
+                rec.pad = kPrimSphere;
+            } else {
+                const igxrt_cube& c = b.d->cubes[t - nt - ns];
+                const float start[3] = {c.xy0[0], c.xy0[1], c.z0_x1[0]};
+                const float end[3] = {c.z0_x1[1], c.yz1[0], c.yz1[1]};
+                for (int a = 0; a < 3; ++a) {
+                    rec.p0[a] = start[a];
+                    rec.e1[a] = end[a];
+                }
+                rec.pad = kPrimCube;
             }
             rec.prim = t;
             rec.leaf_end = (k + 1 == nd.count) ? 1u : 0u;
-            rec.pad = 0;
             out.prims.push_back(rec);
         }
         return ~(int32_t)first;
@@ -393,17 +411,28 @@ uint32_t stack_bound4(const std::vector<igxrt_bvh4_node>& n, int32_t i) {
 
 igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count, const igxrt_build_options* opts,
                        igxrt_bvh& out, std::string& err) {
+    igxrt_scene_desc d{};
+    d.triangles = tris;
+    d.triangle_count = count;
+    return build_bvh_mixed(d, opts, out, err);
+}
+
+igxrt_status build_bvh_mixed(const igxrt_scene_desc& d, const igxrt_build_options* opts,
+                             igxrt_bvh& out, std::string& err) {
     out = igxrt_bvh{};
-    if (count > 0 && !tris) {
-        err = "triangles pointer is NULL";
+    if ((d.triangle_count && !d.triangles) || (d.sphere_count && !d.spheres) ||
+        (d.cube_count && !d.cubes) || (d.plane_count && !d.planes)) {
+        err = "a primitive buffer with a non-zero count is NULL";
         return IGXRT_ERROR_INVALID_ARGUMENT;
     }
-    if (count >= 0x7fffffffu) {
-        err = "too many triangles";
+    const uint64_t total = (uint64_t)d.triangle_count + d.sphere_count + d.cube_count;
+    if (total + d.plane_count >= 0x7fffffffu) {
+        err = "too many primitives";
         return IGXRT_ERROR_INVALID_ARGUMENT;
     }
+    const uint32_t count = (uint32_t)total;  // primitives in the tree
     Builder b;
-    b.tris = tris;
+    b.d = &d;
     b.n = count;
     if (opts) {
         if (opts->max_leaf_size)
@@ -427,7 +456,17 @@ igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count, const igxrt_b
     unsigned threads = (opts && opts->threads) ? opts->threads : (hw ? hw : 1);
     b.spare_threads = (int)threads - 1;
 
-    out.tris.assign(tris, tris + count);
+    const uint32_t nt = d.triangle_count, ns = d.sphere_count, nc = d.cube_count;
+    out.tris.assign(d.triangles, d.triangles + nt);
+    out.spheres.assign(d.spheres, d.spheres + 4 * (size_t)ns);
+    out.cubes.assign(d.cubes, d.cubes + nc);
+    out.planes.assign(d.planes, d.planes + 4 * (size_t)d.plane_count);
+    for (float v : out.planes)
+        if (!std::isfinite(v)) {
+            err = "a plane has a non-finite coefficient";
+            out = igxrt_bvh{};
+            return IGXRT_ERROR_INVALID_ARGUMENT;
+        }
     Aabb scene;
     scene.reset();
     float maxabs = 0.f;
@@ -435,14 +474,41 @@ igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count, const igxrt_b
     b.cen.resize(3 * (size_t)count);
     b.refs.resize(count);
     for (uint32_t i = 0; i < count; ++i) {
-        const igxrt_triangle& t = tris[i];
+        float v[3][3];
+        int nv;
+        if (i < nt) {
+            const igxrt_triangle& t = d.triangles[i];
+            for (int c = 0; c < 3; ++c) {
+                v[0][c] = t.p0[c];
+                v[1][c] = t.p1[c];
+                v[2][c] = t.p2[c];
+            }
+            nv = 3;
+        } else if (i < nt + ns) {
+            // the sphere's box: centre -/+ |radius| (the test squares the radius)
+            const float* s = d.spheres + 4 * (size_t)(i - nt);
+            const float r = std::fabs(s[3]);
+            for (int c = 0; c < 3; ++c) {  // a non-finite radius fails the check below
+                v[0][c] = s[c] - r;
+                v[1][c] = s[c] + r;
+            }
+            nv = 2;
+        } else {
+            const igxrt_cube& cb = d.cubes[i - nt - ns];
+            const float start[3] = {cb.xy0[0], cb.xy0[1], cb.z0_x1[0]};
+            const float end[3] = {cb.z0_x1[1], cb.yz1[0], cb.yz1[1]};
+            for (int c = 0; c < 3; ++c) {
+                v[0][c] = start[c];
+                v[1][c] = end[c];
+            }
+            nv = 2;
+        }
         Aabb a;
         a.reset();
-        const float* v[3] = {t.p0, t.p1, t.p2};
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < nv; ++k) {
             for (int c = 0; c < 3; ++c) {
                 if (!std::isfinite(v[k][c])) {
-                    err = format("triangle %u has a non-finite vertex coordinate", i);
+                    err = format("primitive %u has a non-finite coordinate", i);
                     out = igxrt_bvh{};
                     return IGXRT_ERROR_INVALID_ARGUMENT;
                 }
@@ -458,7 +524,10 @@ igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count, const igxrt_b
     }
 
     igxrt_bvh_info& info = out.info;
-    info.triangle_count = count;
+    info.triangle_count = nt;
+    info.sphere_count = ns;
+    info.cube_count = nc;
+    info.plane_count = d.plane_count;
     info.max_leaf_size = b.max_leaf;
     const float pad = std::max(maxabs * 0x1p-18f, 1e-30f);
     info.pad_abs = pad;
@@ -517,7 +586,8 @@ igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count, const igxrt_b
     info.device_bytes = sizeof(igxrt_bvh2_node) * out.nodes2.size() +
                         sizeof(igxrt_bvh4_node) * out.nodes4.size() +
                         sizeof(igxrt_prim_record) * out.prims.size() +
-                        sizeof(igxrt_triangle) * out.tris.size();
+                        sizeof(igxrt_triangle) * out.tris.size() +
+                        sizeof(float) * out.planes.size();
     return IGXRT_OK;
 }
 
@@ -557,18 +627,42 @@ struct Checker {
                 return fail(format("primitive record %llu reached twice", (unsigned long long)i));
             rec_seen[i] = 1;
             const igxrt_prim_record& r = b.prims[i];
-            if (r.prim >= b.tris.size())
-                return fail(format("record %llu names triangle %u", (unsigned long long)i, r.prim));
-            const igxrt_triangle& t = b.tris[r.prim];
-            for (int a = 0; a < 3; ++a) {
-                const float e1 = t.p1[a] - t.p0[a], e2 = t.p2[a] - t.p0[a];
-                if (memcmp(&r.p0[a], &t.p0[a], 4) || memcmp(&r.e1[a], &e1, 4) ||
-                    memcmp(&r.e2[a], &e2, 4))
-                    return fail(format("record %llu does not match triangle %u",
-                                       (unsigned long long)i, r.prim));
+            const size_t nt = b.tris.size(), ns = b.spheres.size() / 4, nc = b.cubes.size();
+            if (r.prim >= nt + ns + nc)
+                return fail(format("record %llu names object %u", (unsigned long long)i, r.prim));
+            const uint32_t want = r.prim < nt ? kPrimTriangle : r.prim < nt + ns ? kPrimSphere : kPrimCube;
+            if (r.pad != want)
+                return fail(format("record %llu has type %u, object %u needs %u",
+                                   (unsigned long long)i, r.pad, r.prim, want));
+            if (want == kPrimTriangle) {
+                const igxrt_triangle& t = b.tris[r.prim];
+                for (int a = 0; a < 3; ++a) {
+                    const float e1 = t.p1[a] - t.p0[a], e2 = t.p2[a] - t.p0[a];
+                    if (memcmp(&r.p0[a], &t.p0[a], 4) || memcmp(&r.e1[a], &e1, 4) ||
+                        memcmp(&r.e2[a], &e2, 4))
+                        return fail(format("record %llu does not match triangle %u",
+                                           (unsigned long long)i, r.prim));
+                }
+                if (!inside(t.p0, lo, hi) || !inside(t.p1, lo, hi) || !inside(t.p2, lo, hi))
+                    return fail(format("triangle %u outside its leaf box", r.prim));
+            } else if (want == kPrimSphere) {
+                const float* s = &b.spheres[4 * (r.prim - nt)];
+                if (memcmp(r.p0, s, 12) || memcmp(&r.e1[0], &s[3], 4))
+                    return fail(format("record %llu does not match sphere %u", (unsigned long long)i, r.prim));
+                const float rad = std::fabs(s[3]);
+                const float c0[3] = {s[0] - rad, s[1] - rad, s[2] - rad};
+                const float c1[3] = {s[0] + rad, s[1] + rad, s[2] + rad};
+                if (!inside(c0, lo, hi) || !inside(c1, lo, hi))
+                    return fail(format("sphere %u outside its leaf box", r.prim));
+            } else {
+                const igxrt_cube& c = b.cubes[r.prim - nt - ns];
+                const float start[3] = {c.xy0[0], c.xy0[1], c.z0_x1[0]};
+                const float end[3] = {c.z0_x1[1], c.yz1[0], c.yz1[1]};
+                if (memcmp(r.p0, start, 12) || memcmp(r.e1, end, 12))
+                    return fail(format("record %llu does not match cube %u", (unsigned long long)i, r.prim));
+                if (!inside(start, lo, hi) || !inside(end, lo, hi))
+                    return fail(format("cube %u outside its leaf box", r.prim));
             }
-            if (!inside(t.p0, lo, hi) || !inside(t.p1, lo, hi) || !inside(t.p2, lo, hi))
-                return fail(format("triangle %u outside its leaf box", r.prim));
             if (r.leaf_end)
                 break;
         }
@@ -579,9 +673,14 @@ struct Checker {
 }  // namespace
 
 igxrt_status validate_bvh(const igxrt_bvh& b, std::string& msg) {
-    const size_t nt = b.tris.size();
+    // objects in the tree: triangles, spheres, cubes (planes stay outside)
+    if (b.spheres.size() % 4 || b.planes.size() % 4) {
+        msg = "sphere or plane buffer is not a whole number of vec4s";
+        return IGXRT_ERROR_INVALID_BVH;
+    }
+    const size_t nt = b.tris.size() + b.spheres.size() / 4 + b.cubes.size();
     if (b.prims.size() != nt) {
-        msg = format("%zu primitive records for %zu triangles", b.prims.size(), nt);
+        msg = format("%zu primitive records for %zu objects", b.prims.size(), nt);
         return IGXRT_ERROR_INVALID_BVH;
     }
     if (nt == 0) {
@@ -724,8 +823,10 @@ struct FileHeader {
     uint32_t version;
     uint32_t abi;
     uint64_t tris, nodes2, nodes4, prims;
+    uint64_t spheres, cubes, planes;
     igxrt_bvh_info info;
 };
+constexpr uint32_t kFileVersion = 2;
 
 constexpr char kMagic[8] = {'I', 'G', 'X', 'R', 'T', 'B', 'V', 'H'};
 
@@ -745,6 +846,29 @@ igxrt_status igxrt_bvh_build(const igxrt_triangle* tris, uint32_t count,
     igxrt_status st;
     try {
         st = build_bvh(tris, count, opts, *b, err);
+    } catch (const std::bad_alloc&) {
+        st = IGXRT_ERROR_OUT_OF_MEMORY;
+    }
+    if (st != IGXRT_OK) {
+        delete b;
+        return st;
+    }
+    *out = b;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_bvh_build_mixed(const igxrt_scene_desc* desc, const igxrt_build_options* opts,
+                                   igxrt_bvh** out) {
+    if (!out || !desc)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    igxrt_bvh* b = new (std::nothrow) igxrt_bvh();
+    if (!b)
+        return IGXRT_ERROR_OUT_OF_MEMORY;
+    std::string err;
+    igxrt_status st;
+    try {
+        st = build_bvh_mixed(*desc, opts, *b, err);
     } catch (const std::bad_alloc&) {
         st = IGXRT_ERROR_OUT_OF_MEMORY;
     }
@@ -804,18 +928,24 @@ igxrt_status igxrt_bvh_save(const igxrt_bvh* bvh, const char* path) {
         return IGXRT_ERROR_IO;
     FileHeader h{};
     memcpy(h.magic, kMagic, 8);
-    h.version = 1;
+    h.version = kFileVersion;
     h.abi = IGXRT_ABI_VERSION;
     h.tris = bvh->tris.size();
     h.nodes2 = bvh->nodes2.size();
     h.nodes4 = bvh->nodes4.size();
     h.prims = bvh->prims.size();
+    h.spheres = bvh->spheres.size() / 4;
+    h.cubes = bvh->cubes.size();
+    h.planes = bvh->planes.size() / 4;
     h.info = bvh->info;
     bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
     ok = ok && fwrite(bvh->tris.data(), sizeof(igxrt_triangle), h.tris, f) == h.tris;
     ok = ok && fwrite(bvh->nodes2.data(), sizeof(igxrt_bvh2_node), h.nodes2, f) == h.nodes2;
     ok = ok && fwrite(bvh->nodes4.data(), sizeof(igxrt_bvh4_node), h.nodes4, f) == h.nodes4;
     ok = ok && fwrite(bvh->prims.data(), sizeof(igxrt_prim_record), h.prims, f) == h.prims;
+    ok = ok && fwrite(bvh->spheres.data(), 16, h.spheres, f) == h.spheres;
+    ok = ok && fwrite(bvh->cubes.data(), sizeof(igxrt_cube), h.cubes, f) == h.cubes;
+    ok = ok && fwrite(bvh->planes.data(), 16, h.planes, f) == h.planes;
     ok = (fclose(f) == 0) && ok;
     return ok ? IGXRT_OK : IGXRT_ERROR_IO;
 }
@@ -831,10 +961,12 @@ igxrt_status igxrt_bvh_load(const char* path, igxrt_bvh** out) {
     igxrt_bvh* b = nullptr;
     igxrt_status st = IGXRT_ERROR_IO;
     do {
-        if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, kMagic, 8) || h.version != 1)
+        if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, kMagic, 8) || h.version != kFileVersion)
             break;
-        if (h.tris >= 0x7fffffffu || h.prims != h.tris || h.nodes2 > 2 * h.tris + 1 ||
-            h.nodes4 > 2 * h.tris + 1)
+        const uint64_t objects = h.tris + h.spheres + h.cubes;
+        if (h.tris >= 0x7fffffffu || h.spheres >= 0x7fffffffu || h.cubes >= 0x7fffffffu ||
+            h.planes >= 0x7fffffffu || objects + h.planes >= 0x7fffffffu || h.prims != objects ||
+            h.nodes2 > 2 * objects + 1 || h.nodes4 > 2 * objects + 1)
             break;
         b = new (std::nothrow) igxrt_bvh();
         if (!b) {
@@ -845,10 +977,16 @@ igxrt_status igxrt_bvh_load(const char* path, igxrt_bvh** out) {
         b->nodes2.resize(h.nodes2);
         b->nodes4.resize(h.nodes4);
         b->prims.resize(h.prims);
+        b->spheres.resize(4 * h.spheres);
+        b->cubes.resize(h.cubes);
+        b->planes.resize(4 * h.planes);
         if (fread(b->tris.data(), sizeof(igxrt_triangle), h.tris, f) != h.tris ||
             fread(b->nodes2.data(), sizeof(igxrt_bvh2_node), h.nodes2, f) != h.nodes2 ||
             fread(b->nodes4.data(), sizeof(igxrt_bvh4_node), h.nodes4, f) != h.nodes4 ||
-            fread(b->prims.data(), sizeof(igxrt_prim_record), h.prims, f) != h.prims)
+            fread(b->prims.data(), sizeof(igxrt_prim_record), h.prims, f) != h.prims ||
+            fread(b->spheres.data(), 16, h.spheres, f) != h.spheres ||
+            fread(b->cubes.data(), sizeof(igxrt_cube), h.cubes, f) != h.cubes ||
+            fread(b->planes.data(), 16, h.planes, f) != h.planes)
             break;
         b->info = h.info;
         std::string m;

@@ -344,7 +344,8 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
     const size_t b4 = round_up(bvh->nodes4.size() * sizeof(igxrt_bvh4_node), 256);
     const size_t bp = round_up(bvh->prims.size() * sizeof(igxrt_prim_record), 256);
     const size_t bt = round_up(bvh->tris.size() * sizeof(igxrt_triangle), 256);
-    const size_t total = std::max<size_t>(b2 + b4 + bp + bt, 256);
+    const size_t bl = round_up(bvh->planes.size() * sizeof(float), 256);
+    const size_t total = std::max<size_t>(b2 + b4 + bp + bt + bl, 256);
     cudaError_t e = cudaMalloc(&s->d_mem, total);
     if (e != cudaSuccess) {
         delete s;
@@ -357,7 +358,14 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
     s->tris = (const igxrt_triangle*)(base + b2 + b4 + bp);
     s->node_count[IGXRT_LAYOUT_BVH2] = (uint32_t)bvh->nodes2.size();
     s->node_count[IGXRT_LAYOUT_BVH4] = (uint32_t)bvh->nodes4.size();
-    if (!bvh->nodes2.empty())
+    s->mixed = !bvh->spheres.empty() || !bvh->cubes.empty() || !bvh->planes.empty();
+    s->planes = (const float*)(base + b2 + b4 + bp + bt);
+    s->plane_count = (uint32_t)(bvh->planes.size() / 4);
+    s->plane_base = (uint32_t)(bvh->tris.size() + bvh->spheres.size() / 4 + bvh->cubes.size());
+    if (!bvh->planes.empty())
+        e = cudaMemcpy(base + b2 + b4 + bp + bt, bvh->planes.data(), bvh->planes.size() * sizeof(float),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !bvh->nodes2.empty())
         e = cudaMemcpy(base, bvh->nodes2.data(), bvh->nodes2.size() * sizeof(igxrt_bvh2_node), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !bvh->nodes4.empty())
         e = cudaMemcpy(base + b2, bvh->nodes4.data(), bvh->nodes4.size() * sizeof(igxrt_bvh4_node), cudaMemcpyHostToDevice);
@@ -384,6 +392,25 @@ igxrt_status igxrt_scene_create(igxrt_context* ctx, const igxrt_triangle* tris, 
     igxrt_status st;
     try {
         st = build_bvh(tris, count, opts, bvh, err);
+    } catch (const std::bad_alloc&) {
+        st = IGXRT_ERROR_OUT_OF_MEMORY;
+        err = "host memory exhausted during the BVH build";
+    }
+    if (st != IGXRT_OK)
+        return fail(ctx, st, err);
+    return igxrt_scene_create_from_bvh(ctx, &bvh, out);
+}
+
+igxrt_status igxrt_scene_create_mixed(igxrt_context* ctx, const igxrt_scene_desc* desc,
+                                      const igxrt_build_options* opts, igxrt_scene** out) {
+    if (!ctx || !out || !desc)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    igxrt_bvh bvh;
+    std::string err;
+    igxrt_status st;
+    try {
+        st = build_bvh_mixed(*desc, opts, bvh, err);
     } catch (const std::bad_alloc&) {
         st = IGXRT_ERROR_OUT_OF_MEMORY;
         err = "host memory exhausted during the BVH build";
@@ -438,6 +465,8 @@ igxrt_status igxrt_count_fetches(igxrt_context* ctx, const igxrt_scene* scene, c
         return IGXRT_ERROR_INVALID_ARGUMENT;
     if (mode > 1 || layout >= IGXRT_LAYOUT_COUNT || !node_fetches || !prim_fetches)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "mode 0/1, a valid layout and both count arrays");
+    if (scene && scene->mixed)
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "fetch counts are kept for triangle-only scenes");
     if (count == 0)
         return IGXRT_OK;
     // The instrumented kernel also writes the query's results; they go to a

@@ -41,6 +41,11 @@ struct igxrt_scene {
     uint32_t node_count[IGXRT_LAYOUT_COUNT] = {0, 0};
     const igxrt_prim_record* prims = nullptr;
     const igxrt_triangle* tris = nullptr;
+    // mixed scenes: spheres and cubes are in the tree, planes are not
+    bool mixed = false;
+    const float* planes = nullptr;  // 4 floats per plane
+    uint32_t plane_count = 0;
+    uint32_t plane_base = 0;        // object id of the first plane
 };
 
 namespace igxrt {

@@ -140,6 +140,8 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     igxrt_status st = check_scene(ctx, scene);
     if (st != IGXRT_OK)
         return st;
+    if (scene->mixed)
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "the G-buffer pass takes triangle-only scenes");
     if (!cam || !dir_object || !uv_normal)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "camera and both images must be non-NULL");
     if (!cam->width || !cam->height)

@@ -14,8 +14,16 @@
 constexpr uint32_t kMaxDepth = 80;
 constexpr uint32_t kStackCapacity = 128;
 
+// Primitive types, the last word of a primitive record.
+constexpr uint32_t kPrimTriangle = 0;
+constexpr uint32_t kPrimSphere = 1;
+constexpr uint32_t kPrimCube = 2;
+
 struct igxrt_bvh {
     std::vector<igxrt_triangle> tris;
+    std::vector<float> spheres;      // 4 per sphere: centre, radius
+    std::vector<igxrt_cube> cubes;
+    std::vector<float> planes;       // 4 per plane: normal, offset (outside the tree)
     std::vector<igxrt_bvh2_node> nodes2;
     std::vector<igxrt_bvh4_node> nodes4;
     std::vector<igxrt_prim_record> prims;
@@ -30,6 +38,9 @@ std::string format(const char* fmt, ...);
 // Builds `out` from the triangles (host only).
 igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count,
                        const igxrt_build_options* opts, igxrt_bvh& out, std::string& err);
+// Builds `out` from all primitive buffers of a scene (host only).
+igxrt_status build_bvh_mixed(const igxrt_scene_desc& d, const igxrt_build_options* opts,
+                             igxrt_bvh& out, std::string& err);
 
 // Structural validation; returns IGXRT_OK or IGXRT_ERROR_INVALID_BVH with msg.
 igxrt_status validate_bvh(const igxrt_bvh& bvh, std::string& msg);

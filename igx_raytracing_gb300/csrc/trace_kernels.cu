@@ -37,17 +37,21 @@ struct KernelArgs {
     uint32_t packet;
     uint32_t sh_depth;
     uint32_t refill_lanes;
+    const float4* planes;  // mixed scenes: planes outside the tree
+    uint32_t plane_count;
+    uint32_t plane_base;   // object id of the first plane
 };
 
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool MIXED>
 __device__ __forceinline__ void finish_ray(const KernelArgs& a, uint32_t i, const RayState& r,
                                            const BestHit& best, bool occluded, uint32_t nf,
                                            uint32_t pf) {
     if (ANY) {
         __stcs(a.occluded + i, occluded ? 1u : 0u);
     } else {
-        const bool hit = best.t < r.tmax_eff;
-        const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(best.prim))
+        const bool hit = MIXED ? (best.t < r.tmax_eff || best.prim < kPrioNone) : best.t < r.tmax_eff;
+        const uint32_t prim = MIXED ? id_of_prio(best.prim) : best.prim;
+        const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(prim))
                              : make_float4(IGXRT_NO_HIT, 0.f, 0.f, __uint_as_float(IGXRT_NO_RAY_HIT));
         __stcs(reinterpret_cast<float4*>(a.hits) + i, h);
     }
@@ -65,7 +69,9 @@ __device__ __forceinline__ void finish_ray(const KernelArgs& a, uint32_t i, cons
 // packet of `packet` ray indices for the warp, and idle lanes take the next
 // indices in lane order (ballot + popc).  Per ray the sequence of node and
 // leaf visits is exactly the host traversal's (oracle/trace_oracle.c).
-template <int LAYOUT, bool ANY, bool COUNT>
+// MIXED: scenes with spheres, cubes and planes (typed leaves, planes tested
+// when a ray starts, priority-coded best hit).
+template <int LAYOUT, bool ANY, bool COUNT, bool MIXED>
 __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
     extern __shared__ uint32_t smem[];
     TraversalStack st;
@@ -77,7 +83,7 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
     const uint32_t lower = (1u << lane) - 1u;
     uint32_t pk_base = 0, pk_end = 0;  // warp-uniform window of claimed rays
     bool queue_done = false;           // warp-uniform
-    bool alive = false;
+    bool alive = false, occluded_at_start = false;
     uint32_t ray = 0, nf = 0, pf = 0;
     int32_t next = kRefDone;
     RayState r;
@@ -108,9 +114,16 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
                     best.t = r.tmax_eff;
                     best.u = 0.f;
                     best.v = 0.f;
-                    best.prim = 0;  // "prim < best.prim" cannot hold before a first hit
+                    // "prim < best.prim" cannot hold before a first hit
+                    best.prim = MIXED ? kPrioNone : 0u;
                     best.tcull = cull_limit(best.t);
                     next = a.node_count ? 0 : kRefDone;
+                    occluded_at_start = false;
+                    if (MIXED && a.plane_count) {
+                        occluded_at_start = test_planes<ANY>(a.planes, a.plane_count, a.plane_base, r, best);
+                        if (occluded_at_start)
+                            next = kRefDone;
+                    }
                     st.sp = 0;
                     nf = 0;
                     pf = 0;
@@ -126,18 +139,19 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
             bool overflow = false;
             // node phase
             while (next >= 0 && next != kRefDone)
-                next = visit_node<LAYOUT, COUNT>(a.nodes, next, r, best, st, overflow, nf);
-            bool occluded = false;
+                next = visit_node<LAYOUT, COUNT, MIXED>(a.nodes, next, r, best, st, overflow, nf);
+            bool occluded = occluded_at_start;
             // leaf phase
             if (next < 0) {
-                occluded = process_leaf<ANY, COUNT>(a.prims, next, r, best, pf);
+                occluded = MIXED ? process_leaf_mixed<ANY>(a.prims, next, r, best)
+                                 : process_leaf<ANY, COUNT>(a.prims, next, r, best, pf);
                 if (!occluded)
                     next = st.pop_live(best.tcull);
             }
             if (overflow)
                 atomicOr(a.status, kStatusStackOverflow);
             if (occluded || next == kRefDone) {
-                finish_ray<ANY, COUNT>(a, ray, r, best, occluded, nf, pf);
+                finish_ray<ANY, COUNT, MIXED>(a, ray, r, best, occluded, nf, pf);
                 alive = false;
             }
         }
@@ -146,15 +160,23 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
 
 using KernelFn = void (*)(KernelArgs);
 
-static KernelFn select_kernel(uint32_t layout, bool any, bool count) {
-    if (layout == IGXRT_LAYOUT_BVH4) {
+// Instrumented variants exist for triangle-only scenes; mixed scenes have
+// no host traversal to compare counts with.
+static KernelFn select_kernel(uint32_t layout, bool any, bool count, bool mixed) {
+    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4;
+    if (mixed) {
+        if (layout == B4)
+            return any ? trace_kernel<B4, true, false, true> : trace_kernel<B4, false, false, true>;
+        return any ? trace_kernel<B2, true, false, true> : trace_kernel<B2, false, false, true>;
+    }
+    if (layout == B4) {
         if (count)
-            return any ? trace_kernel<IGXRT_LAYOUT_BVH4, true, true> : trace_kernel<IGXRT_LAYOUT_BVH4, false, true>;
-        return any ? trace_kernel<IGXRT_LAYOUT_BVH4, true, false> : trace_kernel<IGXRT_LAYOUT_BVH4, false, false>;
+            return any ? trace_kernel<B4, true, true, false> : trace_kernel<B4, false, true, false>;
+        return any ? trace_kernel<B4, true, false, false> : trace_kernel<B4, false, false, false>;
     }
     if (count)
-        return any ? trace_kernel<IGXRT_LAYOUT_BVH2, true, true> : trace_kernel<IGXRT_LAYOUT_BVH2, false, true>;
-    return any ? trace_kernel<IGXRT_LAYOUT_BVH2, true, false> : trace_kernel<IGXRT_LAYOUT_BVH2, false, false>;
+        return any ? trace_kernel<B2, true, true, false> : trace_kernel<B2, false, true, false>;
+    return any ? trace_kernel<B2, true, false, false> : trace_kernel<B2, false, false, false>;
 }
 
 igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
@@ -163,7 +185,7 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
         return IGXRT_OK;
     const igxrt_scene* s = req.scene;
     const bool count = req.node_fetches != nullptr;
-    KernelFn fn = select_kernel(p.layout, req.mode == 1, count);
+    KernelFn fn = select_kernel(p.layout, req.mode == 1, count, s->mixed);
     const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
     cudaError_t e = allow_smem((const void*)fn, smem);
@@ -196,6 +218,9 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;
+    a.planes = reinterpret_cast<const float4*>(s->planes);
+    a.plane_count = s->plane_count;
+    a.plane_base = s->plane_base;
     e = cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "queue reset");
@@ -212,7 +237,7 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
     if (req.count == 0)
         return IGXRT_OK;
     const igxrt_scene* s = req.scene;
-    KernelFn fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr);
+    KernelFn fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr, s->mixed);
     const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
     cudaError_t e = allow_smem((const void*)fn, smem);
@@ -244,6 +269,9 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;
+    a.planes = reinterpret_cast<const float4*>(s->planes);
+    a.plane_count = s->plane_count;
+    a.plane_base = s->plane_base;
     fn<<<grid, p.block_size, smem, stream>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess)

@@ -19,6 +19,7 @@
 #include <cstdint>
 
 #include "igxrt.h"
+#include "internal.h"
 
 namespace igxrt {
 
@@ -45,10 +46,11 @@ __device__ __forceinline__ float safe_dir(float d) {
     return fabsf(d) < 0x1p-80f ? copysignf(0x1p-80f, d) : d;
 }
 
-// Upper bound used to cull boxes: best t widened by 2^-10 (relative), kept
-// finite so the {+inf} box of an absent child is never entered.
+// Upper bound used to cull boxes: best t widened upward by 2^-10 of its
+// magnitude (t can be negative with a negative tmin or an enclosing cube),
+// kept finite so the {+inf} box of an absent child is never entered.
 __device__ __forceinline__ float cull_limit(float t) {
-    return fminf(__fmaf_rn(t, 0x1p-10f, t), 3.4028235e38f);
+    return fminf(__fmaf_rn(fabsf(t), 0x1p-10f, t), 3.4028235e38f);
 }
 
 __device__ __forceinline__ RayState load_ray(const igxrt_ray* __restrict__ rays, uint32_t i,
@@ -85,6 +87,21 @@ __device__ __forceinline__ bool box_hit(const RayState& r, float lox, float hix,
     const float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tcull));
     tn = tnear;
     return tnear <= tfar;
+}
+
+// Slab test of mixed scenes: the entry distance is not clamped to tmin, so a
+// box around the origin keeps its negative entry distance (a cube around the
+// origin is hit there, and a negative best t must not cull it); boxes wholly
+// behind tmin are still culled.
+__device__ __forceinline__ bool box_hit_mixed(const RayState& r, float lox, float hix, float loy,
+                                              float hiy, float loz, float hiz, float tcull, float& tn) {
+    const float t0x = __fmaf_rn(lox, r.ix, -r.oix), t1x = __fmaf_rn(hix, r.ix, -r.oix);
+    const float t0y = __fmaf_rn(loy, r.iy, -r.oiy), t1y = __fmaf_rn(hiy, r.iy, -r.oiy);
+    const float t0z = __fmaf_rn(loz, r.iz, -r.oiz), t1z = __fmaf_rn(hiz, r.iz, -r.oiz);
+    const float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+    const float tslab = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    tn = tnear;
+    return tslab >= r.tmin_box && tnear <= fminf(tslab, tcull);
 }
 
 // rayIntersectTri's arithmetic on a primitive record {p0,prim}{e1,end}{e2,pad}.
@@ -209,10 +226,17 @@ __device__ __forceinline__ void order2(SlotKey& a, SlotKey& b) {
     }
 }
 
+template <bool MIXED>
+__device__ __forceinline__ bool box_test(const RayState& r, float lox, float hix, float loy,
+                                         float hiy, float loz, float hiz, float tcull, float& tn) {
+    return MIXED ? box_hit_mixed(r, lox, hix, loy, hiy, loz, hiz, tcull, tn)
+                 : box_hit(r, lox, hix, loy, hiy, loz, hiz, tcull, tn);
+}
+
 // One interior-node visit in the kernels' order: test the children, descend
 // into the nearer hit child and push the other.  Returns the next reference
 // (a node, a leaf, or kRefDone), or sets `overflow`.
-template <int LAYOUT, bool COUNT>
+template <int LAYOUT, bool COUNT, bool MIXED = false>
 __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, int32_t node,
                                               const RayState& r, const BestHit& best,
                                               TraversalStack& st, bool& overflow, uint32_t& nf) {
@@ -229,16 +253,16 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
                                   __float_as_int(c.w));
         float tn;
         uint32_t h, m = 0;
-        h = box_hit(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, best.tcull, tn);
+        h = box_test<MIXED>(r,lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, best.tcull, tn);
         m += h;
         SlotKey k0 = {h ? tn : INFINITY, ch.x, 0u};
-        h = box_hit(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, best.tcull, tn);
+        h = box_test<MIXED>(r,lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, best.tcull, tn);
         m += h;
         SlotKey k1 = {h ? tn : INFINITY, ch.y, 1u};
-        h = box_hit(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, best.tcull, tn);
+        h = box_test<MIXED>(r,lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, best.tcull, tn);
         m += h;
         SlotKey k2 = {h ? tn : INFINITY, ch.z, 2u};
-        h = box_hit(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, best.tcull, tn);
+        h = box_test<MIXED>(r,lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, best.tcull, tn);
         m += h;
         SlotKey k3 = {h ? tn : INFINITY, ch.w, 3u};
         if (m == 0)
@@ -268,8 +292,8 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
         ldg256(n + 2, z01, c);
         const int32_t c0 = __float_as_int(c.x), c1 = __float_as_int(c.y);
         float tn0, tn1;
-        const bool h0 = box_hit(r, xy0.x, xy0.y, xy0.z, xy0.w, z01.x, z01.y, best.tcull, tn0);
-        const bool h1 = box_hit(r, xy1.x, xy1.y, xy1.z, xy1.w, z01.z, z01.w, best.tcull, tn1);
+        const bool h0 = box_test<MIXED>(r,xy0.x, xy0.y, xy0.z, xy0.w, z01.x, z01.y, best.tcull, tn0);
+        const bool h1 = box_test<MIXED>(r,xy1.x, xy1.y, xy1.z, xy1.w, z01.z, z01.w, best.tcull, tn1);
         if (h0 && h1) {
             const bool first1 = tn1 < tn0;
             if (st.sp >= kStackCapacityDevice) {
@@ -285,6 +309,202 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
             return c1;
         return st.pop_live(best.tcull);
     }
+}
+
+// ---- mixed scenes: spheres, cubes, planes ---------------------------------
+//
+// In mixed scenes BestHit.prim holds a priority instead of the object id:
+// at equal t a lower priority wins.  Cubes accept ties (the cube test rejects
+// only tmin > hit.hitT, primitive.glsl:302) so among the linear loop's
+// candidates at the smallest t the last cube wins, and without a cube the
+// first other object wins: cube id i -> 0x7fffffff - i, other id i ->
+// 0x80000000 + i, and the "no hit yet" state is 0x80000000 (a non-cube needs
+// t < tmax, a cube t <= tmax).
+constexpr uint32_t kPrioNone = 0x80000000u;
+__device__ __forceinline__ uint32_t prio_other(uint32_t id) { return 0x80000000u + id; }
+__device__ __forceinline__ uint32_t prio_cube(uint32_t id) { return 0x7fffffffu - id; }
+__device__ __forceinline__ uint32_t id_of_prio(uint32_t p) {
+    return p >= 0x80000000u ? p - 0x80000000u : 0x7fffffffu - p;
+}
+__device__ __forceinline__ bool better(float t, uint32_t p, const BestHit& b) {
+    return t < b.t || (t == b.t && p < b.prim);
+}
+
+// GLSL min / max as the specification defines them (NaN handling included).
+__device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
+__device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// rayIntersectSphere (primitive.glsl:173-210): hitT and the in-sphere test.
+__device__ __forceinline__ bool sphere_hit(const RayState& r, float cx, float cy, float cz, float rad,
+                                           float& hitT) {
+    const float dx = __fsub_rn(cx, r.ox), dy = __fsub_rn(cy, r.oy), dz = __fsub_rn(cz, r.oz);
+    const float t = dot3f(dx, dy, dz, r.dx, r.dy, r.dz);
+    const float qx = __fsub_rn(dx, __fmul_rn(t, r.dx)), qy = __fsub_rn(dy, __fmul_rn(t, r.dy)),
+                qz = __fsub_rn(dz, __fmul_rn(t, r.dz));
+    const float Q2 = dot3f(qx, qy, qz, qx, qy, qz);
+    const float R2 = __fmul_rn(rad, rad);
+    hitT = __fsub_rn(t, __fsqrt_rn(__fsub_rn(R2, Q2)));
+    return !(Q2 > R2);
+}
+
+// The sphere's uv (primitive.glsl:189-204); asin/atan are CUDA's.
+__device__ __forceinline__ void sphere_uv(const RayState& r, float cx, float cy, float cz, float hitT,
+                                          float& u, float& v) {
+    const float ox = __fadd_rn(__fmul_rn(hitT, r.dx), r.ox), oy = __fadd_rn(__fmul_rn(hitT, r.dy), r.oy),
+                oz = __fadd_rn(__fmul_rn(hitT, r.dz), r.oz);
+    const float nx = __fsub_rn(cx, ox), ny = __fsub_rn(cy, oy), nz = __fsub_rn(cz, oz);
+    const float len = __fsqrt_rn(dot3f(nx, ny, nz, nx, ny, nz));
+    const float ux = __fdiv_rn(nx, len), uy = __fdiv_rn(ny, len), uz = __fdiv_rn(nz, len);
+    const float lat = asinf(uz);
+    float lon = atanf(__fdiv_rn(uy, ux));
+    if (lon != lon)
+        lon = 0.f;
+    const float k = (float)(0.636619746685 * 0.5);
+    u = __fadd_rn(__fmul_rn(lat, k), 0.5f);
+    v = __fadd_rn(__fmul_rn(lon, k), 0.5f);
+}
+
+// rayIntersectCube (primitive.glsl:286-333) with the ray's raw 1/dir.
+// Returns whether [tmin, tmax] is a valid interval reaching tmin_ray.
+__device__ __forceinline__ bool cube_hit(const RayState& r, const float4& s, const float4& e, float& tmin,
+                                         float& u, float& v) {
+    const float rx = __frcp_rn(r.dx), ry = __frcp_rn(r.dy), rz = __frcp_rn(r.dz);
+    const float sx = __fmul_rn(__fsub_rn(s.x, r.ox), rx), sy = __fmul_rn(__fsub_rn(s.y, r.oy), ry),
+                sz = __fmul_rn(__fsub_rn(s.z, r.oz), rz);
+    const float ex = __fmul_rn(__fsub_rn(e.x, r.ox), rx), ey = __fmul_rn(__fsub_rn(e.y, r.oy), ry),
+                ez = __fmul_rn(__fsub_rn(e.z, r.oz), rz);
+    const float mix = gmin(sx, ex), miy = gmin(sy, ey), miz = gmin(sz, ez);
+    const float max_ = gmax(sx, ex), may = gmax(sy, ey), maz = gmax(sz, ez);
+    tmin = gmax(gmax(mix, miy), miz);
+    const float tmax = gmin(gmin(max_, may), maz);
+    if (tmax < r.tmin || tmin > tmax)
+        return false;
+    // pos = (dir * tmin + pos) - start; pos /= end
+    const float px = __fdiv_rn(__fsub_rn(__fadd_rn(__fmul_rn(r.dx, tmin), r.ox), s.x), e.x);
+    const float py = __fdiv_rn(__fsub_rn(__fadd_rn(__fmul_rn(r.dy, tmin), r.oy), s.y), e.y);
+    const float pz = __fdiv_rn(__fsub_rn(__fadd_rn(__fmul_rn(r.dz, tmin), r.oz), s.z), e.z);
+    if (tmin == mix) {
+        u = py;
+        v = pz;
+    } else if (tmin == miy) {
+        u = px;
+        v = pz;
+    } else {
+        u = px;
+        v = py;
+    }
+    return true;
+}
+
+// rayIntersectPlane (primitive.glsl:212-237): hitT, and the uv on request.
+__device__ __forceinline__ float plane_hit(const RayState& r, const float4& pl) {
+    const float len = __fsqrt_rn(dot3f(pl.x, pl.y, pl.z, pl.x, pl.y, pl.z));
+    const float nx = -__fdiv_rn(pl.x, len), ny = -__fdiv_rn(pl.y, len), nz = -__fdiv_rn(pl.z, len);
+    const float dif = dot3f(r.dx, r.dy, r.dz, nx, ny, nz);
+    return __fdiv_rn(-__fadd_rn(dot3f(r.ox, r.oy, r.oz, nx, ny, nz), pl.w), dif);
+}
+
+__device__ __forceinline__ void plane_uv(const RayState& r, const float4& pl, float hitT, float& u,
+                                         float& v) {
+    const float ox = __fadd_rn(__fmul_rn(hitT, r.dx), r.ox), oy = __fadd_rn(__fmul_rn(hitT, r.dy), r.oy),
+                oz = __fadd_rn(__fmul_rn(hitT, r.dz), r.oz);
+    // planeX = cross(n, (0,0,1)), planeZ = cross(n, (1,0,0)) in GLSL component order
+    const float xx = __fsub_rn(__fmul_rn(pl.y, 1.0f), __fmul_rn(0.0f, pl.z));
+    const float xy = __fsub_rn(__fmul_rn(pl.z, 0.0f), __fmul_rn(1.0f, pl.x));
+    const float xz = __fsub_rn(__fmul_rn(pl.x, 0.0f), __fmul_rn(0.0f, pl.y));
+    const float zx = __fsub_rn(__fmul_rn(pl.y, 0.0f), __fmul_rn(0.0f, pl.z));
+    const float zy = __fsub_rn(__fmul_rn(pl.z, 1.0f), __fmul_rn(0.0f, pl.x));
+    const float zz = __fsub_rn(__fmul_rn(pl.x, 0.0f), __fmul_rn(1.0f, pl.y));
+    u = dot3f(ox, oy, oz, xx, xy, xz);
+    v = dot3f(ox, oy, oz, zx, zy, zz);
+}
+
+// Leaf of a mixed scene.  Returns true when an any-hit query is decided.
+template <bool ANY>
+__device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ prims, int32_t ref,
+                                                   const RayState& r, BestHit& best) {
+    uint32_t i = (uint32_t)~ref;
+    for (;;) {
+        const float4* p = prims + 3 * (size_t)i;
+        const float4 v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
+        const uint32_t type = __float_as_uint(v2.w), id = __float_as_uint(v0.w);
+        if (id != r.prev) {
+            if (type == kPrimTriangle) {
+                float t, u, v;
+                if (tri_test(r, v0, v1, v2, t, u, v) && !(t <= r.tmin)) {
+                    if (ANY) {
+                        if (t < r.tmax_eff)
+                            return true;
+                    } else if (better(t, prio_other(id), best)) {
+                        best.t = t;
+                        best.u = u;
+                        best.v = v;
+                        best.prim = prio_other(id);
+                        best.tcull = cull_limit(t);
+                    }
+                }
+            } else if (type == kPrimSphere) {
+                float t;
+                if (sphere_hit(r, v0.x, v0.y, v0.z, v1.x, t) && t >= r.tmin) {
+                    if (ANY) {
+                        if (t < r.tmax_eff)
+                            return true;
+                    } else if (better(t, prio_other(id), best)) {
+                        sphere_uv(r, v0.x, v0.y, v0.z, t, best.u, best.v);
+                        best.t = t;
+                        best.prim = prio_other(id);
+                        best.tcull = cull_limit(t);
+                    }
+                }
+            } else {
+                float t, u, v;
+                if (cube_hit(r, v0, v1, t, u, v)) {
+                    if (ANY) {
+                        if (t < r.tmax_eff)
+                            return true;
+                    } else if (better(t, prio_cube(id), best)) {
+                        best.t = t;
+                        best.u = u;
+                        best.v = v;
+                        best.prim = prio_cube(id);
+                        best.tcull = cull_limit(t);
+                    }
+                }
+            }
+        }
+        if (__float_as_uint(v1.w))
+            break;
+        ++i;
+    }
+    return false;
+}
+
+// Planes of a mixed scene (outside the tree): every ray tests all of them.
+template <bool ANY>
+__device__ __forceinline__ bool test_planes(const float4* __restrict__ planes, uint32_t count,
+                                            uint32_t base, const RayState& r, BestHit& best) {
+    for (uint32_t j = 0; j < count; ++j) {
+        const uint32_t id = base + j;
+        if (id == r.prev)
+            continue;
+        const float4 pl = __ldg(planes + j);
+        const float t = plane_hit(r, pl);
+        if (!(t >= r.tmin))
+            continue;
+        if (ANY) {
+            if (t < r.tmax_eff)
+                return true;
+        } else if (better(t, prio_other(id), best)) {
+            plane_uv(r, pl, t, best.u, best.v);
+            best.t = t;
+            best.prim = prio_other(id);
+            best.tcull = cull_limit(t);
+        }
+    }
+    return false;
 }
 
 // Whole traversal of one ray by one thread (no refill), in the same order as

@@ -155,6 +155,32 @@ typedef struct igxrt_prim_record {
     uint32_t pad;
 } igxrt_prim_record;
 
+/* std430 layout of GLSL `struct Cube` (primitive.glsl:40-44): corners
+ * start = (xy0[0], xy0[1], z0_x1[0]), end = (z0_x1[1], yz1[0], yz1[1]). */
+typedef struct igxrt_cube {
+    float xy0[2];
+    float z0_x1[2];
+    float yz1[2];
+} igxrt_cube;
+
+/*
+ * All primitive buffers of a reference scene (res/shaders/scene.glsl:22-39):
+ * triangles, spheres (4 floats: centre xyz, radius w), cubes and planes
+ * (4 floats: normal xyz, offset w).  Object ids are global in that order:
+ * triangle i is i, sphere i is triangle_count + i, and so on
+ * (the loops of trace.glsl:22-46).
+ */
+typedef struct igxrt_scene_desc {
+    const igxrt_triangle* triangles;
+    uint32_t triangle_count;
+    uint32_t sphere_count;
+    const float* spheres;
+    const igxrt_cube* cubes;
+    uint32_t cube_count;
+    uint32_t plane_count;
+    const float* planes;
+} igxrt_scene_desc;
+
 typedef struct igxrt_build_options {
     uint32_t max_leaf_size; /* 0 = 8; at most 16 */
     uint32_t sah_bins;      /* 0 = 32 */
@@ -176,6 +202,8 @@ typedef struct igxrt_bvh_info {
     float pad_abs;   /* absolute outward padding added to every node box */
     uint32_t max_stack[IGXRT_LAYOUT_COUNT]; /* deepest traversal stack per layout */
     uint64_t device_bytes;
+    uint32_t sphere_count, cube_count, plane_count;
+    uint32_t reserved;
 } igxrt_bvh_info;
 
 typedef struct igxrt_bvh igxrt_bvh;
@@ -188,6 +216,13 @@ typedef struct igxrt_scene igxrt_scene;
  * Rejects non-finite vertex coordinates with IGXRT_ERROR_INVALID_ARGUMENT. */
 igxrt_status igxrt_bvh_build(const igxrt_triangle* tris, uint32_t count,
                              const igxrt_build_options* opts, igxrt_bvh** out);
+/* Builds one BVH over triangles, spheres and cubes of a mixed scene; planes
+ * are unbounded and stay outside the tree (tested by every ray).  Primitive
+ * records of spheres hold {centre, id}{radius, 0, 0, leaf_end}{0, 0, 0, 1},
+ * of cubes {start, id}{end, leaf_end}{0, 0, 0, 2}; the last word of a
+ * record is its type (0 triangle, 1 sphere, 2 cube). */
+igxrt_status igxrt_bvh_build_mixed(const igxrt_scene_desc* desc, const igxrt_build_options* opts,
+                                   igxrt_bvh** out);
 igxrt_status igxrt_bvh_destroy(igxrt_bvh* bvh);
 igxrt_status igxrt_bvh_get_info(const igxrt_bvh* bvh, igxrt_bvh_info* info);
 /* Borrowed pointers to the node array of `layout` and the primitive records;
@@ -216,6 +251,16 @@ const char* igxrt_status_string(igxrt_status status);
 igxrt_status igxrt_scene_create(igxrt_context* ctx, const igxrt_triangle* tris,
                                 uint32_t count, const igxrt_build_options* opts,
                                 igxrt_scene** out);
+/* Builds and uploads a mixed scene.  igxrt_trace_closest and igxrt_trace_any
+ * then follow the reference's rules per primitive type (rayIntersectSphere,
+ * rayIntersectCube, rayIntersectPlane, primitive.glsl:173-333): a sphere hit
+ * needs t >= tmin, a plane hit t >= tmin, a cube hit only tmax >= tmin (a
+ * cube around the origin is hit at its negative entry distance), and at equal
+ * t a cube beats any other primitive and the later of two cubes wins (the
+ * cube test rejects only tmin > hit.hitT).  The batched, shadow-mask and
+ * G-buffer calls take triangle-only scenes. */
+igxrt_status igxrt_scene_create_mixed(igxrt_context* ctx, const igxrt_scene_desc* desc,
+                                      const igxrt_build_options* opts, igxrt_scene** out);
 /* Uploads an already built BVH. */
 igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bvh,
                                          igxrt_scene** out);

@@ -89,6 +89,21 @@ void orc_gbuffer(const igxrt_triangle* tris, uint32_t ntri, const igxrt_camera* 
 void orc_decode_spheremap(uint32_t n, float out[3]);
 void orc_encode_normal(const float n[3], uint32_t out[2]);
 
+/*
+ * traceGeometry / traceOcclusion over all primitive buffers of a scene
+ * (res/shaders/trace.glsl:22-46, 77-95): triangles, spheres, cubes and planes
+ * in global index order with rayIntersectTri / Sphere / Cube / Plane
+ * (primitive.glsl:173-333), brute force.  `tmin` of each ray generalises the
+ * reference's zero bound as the engine does (t > tmin for triangles,
+ * hitT >= tmin for spheres and planes, tmax >= tmin for cubes).
+ */
+void orc_trace_geometry_mixed(const igxrt_scene_desc* scene, const igxrt_ray* rays,
+                              const uint32_t* prev_hit, uint32_t nrays, igxrt_hit* out,
+                              uint32_t* flags, int threads);
+void orc_trace_occlusion_mixed(const igxrt_scene_desc* scene, const igxrt_ray* rays,
+                               const uint32_t* prev_hit, uint32_t nrays, uint32_t* out,
+                               uint32_t* flags, int threads);
+
 /* Number of hardware threads the oracle uses for threads <= 0. */
 int orc_hardware_threads(void);
 

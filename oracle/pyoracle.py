@@ -68,6 +68,10 @@ def lib() -> C.CDLL:
         h.orc_decode_spheremap.restype = None
         h.orc_encode_normal.argtypes = [vp, vp]
         h.orc_encode_normal.restype = None
+        h.orc_trace_geometry_mixed.argtypes = [vp, vp, vp, u32, vp, vp, i32]
+        h.orc_trace_geometry_mixed.restype = None
+        h.orc_trace_occlusion_mixed.argtypes = [vp, vp, vp, u32, vp, vp, i32]
+        h.orc_trace_occlusion_mixed.restype = None
         h.orc_hardware_threads.argtypes = []
         h.orc_hardware_threads.restype = i32
         _lib = h
@@ -202,6 +206,51 @@ def ref_encode_normal(normals) -> np.ndarray:
     out = np.zeros((len(n), 2), dtype=np.uint32)
     ref_lib().igxref_encode_normal(_ptr(n), len(n), _ptr(out))
     return out
+
+
+class _SceneDesc(C.Structure):
+    _fields_ = [("triangles", C.c_void_p), ("triangle_count", C.c_uint32),
+                ("sphere_count", C.c_uint32), ("spheres", C.c_void_p), ("cubes", C.c_void_p),
+                ("cube_count", C.c_uint32), ("plane_count", C.c_uint32), ("planes", C.c_void_p)]
+
+
+def scene_desc(tris=None, spheres=None, cubes=None, planes=None):
+    """An igxrt_scene_desc over numpy arrays (kept alive in the returned tuple)."""
+    keep = [None if a is None else np.ascontiguousarray(a) for a in (tris, spheres, cubes, planes)]
+    d = _SceneDesc()
+    d.triangles, d.triangle_count = _ptr(keep[0]), 0 if keep[0] is None else len(keep[0])
+    d.spheres, d.sphere_count = _ptr(keep[1]), 0 if keep[1] is None else len(keep[1])
+    d.cubes, d.cube_count = _ptr(keep[2]), 0 if keep[2] is None else len(keep[2])
+    d.planes, d.plane_count = _ptr(keep[3]), 0 if keep[3] is None else len(keep[3])
+    return d, keep
+
+
+def trace_geometry_mixed(rays, prev=None, tris=None, spheres=None, cubes=None, planes=None,
+                         threads: int = 0):
+    d, keep = scene_desc(tris, spheres, cubes, planes)
+    rays = np.ascontiguousarray(rays)
+    n = len(rays)
+    out = np.zeros(n, dtype=HIT_DTYPE)
+    flags = np.zeros(n, dtype=np.uint32)
+    p = _prev(prev, n)
+    if n:
+        lib().orc_trace_geometry_mixed(C.addressof(d), _ptr(rays), _ptr(p), n, _ptr(out),
+                                       _ptr(flags), threads)
+    return out, flags
+
+
+def trace_occlusion_mixed(rays, prev=None, tris=None, spheres=None, cubes=None, planes=None,
+                          threads: int = 0):
+    d, keep = scene_desc(tris, spheres, cubes, planes)
+    rays = np.ascontiguousarray(rays)
+    n = len(rays)
+    out = np.zeros(n, dtype=np.uint32)
+    flags = np.zeros(n, dtype=np.uint32)
+    p = _prev(prev, n)
+    if n:
+        lib().orc_trace_occlusion_mixed(C.addressof(d), _ptr(rays), _ptr(p), n, _ptr(out),
+                                        _ptr(flags), threads)
+    return out, flags
 
 
 def reintersect_f64(ray: np.ndarray, tri: np.ndarray):

@@ -263,6 +263,202 @@ void orc_trace_occlusion(const igxrt_triangle* tris, uint32_t ntri, const igxrt_
     run_parallel(brute_any_chunk, &c, nrays, 64, threads);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Spheres, cubes and planes (mixed scenes).                                */
+/* ------------------------------------------------------------------------ */
+
+/* GLSL min / max as the specification defines them. */
+static inline float gmin(float x, float y) { return y < x ? y : x; }
+static inline float gmax(float x, float y) { return x < y ? y : x; }
+static inline v3 scale(v3 a, float s) {
+    v3 r = {a.x * s, a.y * s, a.z * s};
+    return r;
+}
+static inline v3 add(v3 a, v3 b) {
+    v3 r = {a.x + b.x, a.y + b.y, a.z + b.z};
+    return r;
+}
+static inline v3 normalize3(v3 a) {
+    const float len = sqrtf(dot(a, a));
+    v3 r = {a.x / len, a.y / len, a.z / len};
+    return r;
+}
+
+/* rayIntersectSphere, res/shaders/primitive.glsl:173-210. */
+static int ray_intersect_sphere(v3 pos, v3 dir, float tmin, const float* sphere, uint64_t obj,
+                                uint64_t prevObj, hitstate* hit) {
+    const v3 c = mk(sphere);
+    const v3 dif = sub(c, pos);                /* :175 */
+    const float t = dot(dif, dir);             /* :176 */
+    const v3 Q = sub(dif, scale(dir, t));      /* :178 */
+    const float Q2 = dot(Q, Q);                /* :179 */
+    const float R2 = sphere[3] * sphere[3];    /* :180 */
+    const int outOfSphere = Q2 > R2;           /* :182 */
+    const float hitT = t - sqrtf(R2 - Q2);     /* :183 */
+    if (!outOfSphere && obj != prevObj && hitT >= tmin && hitT < hit->hitT) { /* :185 */
+        hit->hitT = hitT;
+        const v3 o = add(scale(dir, hitT), pos);          /* :189 */
+        const v3 normal = normalize3(sub(c, o));          /* :190 */
+        const float latitude = asinf(normal.z);           /* :198 */
+        float longitude = atanf(normal.y / normal.x);     /* :199 */
+        if (longitude != longitude)                       /* :201-202 */
+            longitude = 0;
+        const float k = (float)(0.636619746685 * 0.5);    /* :204 */
+        hit->u = latitude * k + 0.5f;
+        hit->v = longitude * k + 0.5f;
+        return 1;
+    }
+    return 0;
+}
+
+/* rayIntersectPlane, res/shaders/primitive.glsl:212-237. */
+static int ray_intersect_plane(v3 pos, v3 dir, float tmin, const float* plane, uint64_t obj,
+                               uint64_t prevObj, hitstate* hit) {
+    const v3 n = mk(plane);
+    const v3 pdir = normalize3(n);                      /* :214 */
+    const v3 neg = {-pdir.x, -pdir.y, -pdir.z};
+    const float dif = dot(dir, neg);                    /* :215 */
+    const float hitT = -(dot(pos, neg) + plane[3]) / dif; /* :219 */
+    if (hitT >= tmin && obj != prevObj && hitT < hit->hitT) { /* :221 */
+        hit->hitT = hitT;
+        const v3 o = add(scale(dir, hitT), pos);        /* :226 */
+        const v3 z = {0, 0, 1}, x = {1, 0, 0};
+        const v3 planeX = cross(n, z);                  /* :228 */
+        const v3 planeZ = cross(n, x);                  /* :229 */
+        hit->u = dot(o, planeX);                        /* :231 */
+        hit->v = dot(o, planeZ);
+        return 1;
+    }
+    return 0;
+}
+
+/* rayIntersectCube, res/shaders/primitive.glsl:286-333. */
+static int ray_intersect_cube(v3 pos, v3 dir, float tmin_ray, const igxrt_cube* cube, uint64_t obj,
+                              uint64_t prevObj, hitstate* hit) {
+    const v3 revDir = {1 / dir.x, 1 / dir.y, 1 / dir.z};               /* :288 */
+    const v3 start = {cube->xy0[0], cube->xy0[1], cube->z0_x1[0]};     /* :290 */
+    const v3 end = {cube->z0_x1[1], cube->yz1[0], cube->yz1[1]};       /* :291 */
+    const v3 sd = sub(start, pos), ed = sub(end, pos);
+    const v3 startDir = {sd.x * revDir.x, sd.y * revDir.y, sd.z * revDir.z}; /* :293 */
+    const v3 endDir = {ed.x * revDir.x, ed.y * revDir.y, ed.z * revDir.z};
+    const v3 mi = {gmin(startDir.x, endDir.x), gmin(startDir.y, endDir.y), gmin(startDir.z, endDir.z)};
+    const v3 ma = {gmax(startDir.x, endDir.x), gmax(startDir.y, endDir.y), gmax(startDir.z, endDir.z)};
+    const float tmin = gmax(gmax(mi.x, mi.y), mi.z);    /* :299 */
+    const float tmax = gmin(gmin(ma.x, ma.y), ma.z);    /* :300 */
+    if (tmax < tmin_ray || tmin > tmax || tmin > hit->hitT || obj == prevObj) /* :302 */
+        return 0;
+    v3 p = sub(add(scale(dir, tmin), pos), start);      /* :308 */
+    p.x = p.x / end.x;                                  /* :309 */
+    p.y = p.y / end.y;
+    p.z = p.z / end.z;
+    if (tmin == mi.x) {                                 /* :311-327 */
+        hit->u = p.y;
+        hit->v = p.z;
+    } else if (tmin == mi.y) {
+        hit->u = p.x;
+        hit->v = p.z;
+    } else {
+        hit->u = p.x;
+        hit->v = p.y;
+    }
+    hit->hitT = tmin;                                   /* :331 */
+    return 1;
+}
+
+/* The loops of traceGeometry / traceOcclusion over every buffer
+ * (trace.glsl:22-46, 75-95); returns whether anything was accepted. */
+static int trace_mixed_one(const igxrt_scene_desc* d, const igxrt_ray* ray, uint32_t prev,
+                           hitstate* hit) {
+    const v3 pos = mk(ray->org), dir = mk(ray->dir);
+    const uint64_t p = prev;
+    int found = 0;
+    uint32_t j = 0;
+    for (uint32_t i = 0; i < d->triangle_count; ++i, ++j)
+        if (ray_intersect_tri(pos, dir, ray->tmin, &d->triangles[i], j, p, hit)) {
+            hit->object = j;
+            found = 1;
+        }
+    for (uint32_t i = 0; i < d->sphere_count; ++i, ++j)
+        if (ray_intersect_sphere(pos, dir, ray->tmin, d->spheres + 4 * (size_t)i, j, p, hit)) {
+            hit->object = j;
+            found = 1;
+        }
+    for (uint32_t i = 0; i < d->cube_count; ++i, ++j)
+        if (ray_intersect_cube(pos, dir, ray->tmin, &d->cubes[i], j, p, hit)) {
+            hit->object = j;
+            found = 1;
+        }
+    for (uint32_t i = 0; i < d->plane_count; ++i, ++j)
+        if (ray_intersect_plane(pos, dir, ray->tmin, d->planes + 4 * (size_t)i, j, p, hit)) {
+            hit->object = j;
+            found = 1;
+        }
+    return found;
+}
+
+typedef struct {
+    const igxrt_scene_desc* d;
+    const igxrt_ray* rays;
+    const uint32_t* prev;
+    igxrt_hit* hits;
+    uint32_t* occ;
+    uint32_t* flags;
+} mixed_ctx;
+
+static void mixed_closest_chunk(void* p, uint32_t b, uint32_t e) {
+    mixed_ctx* c = (mixed_ctx*)p;
+    for (uint32_t i = b; i < e; ++i) {
+        hitstate hit;
+        hit.hitT = tmax_effective(c->rays[i].tmax);
+        hit.u = hit.v = 0;
+        hit.object = 0;
+        hit.events = 0;
+        const int found = trace_mixed_one(c->d, &c->rays[i], c->prev ? c->prev[i] : IGXRT_NO_RAY_HIT, &hit);
+        igxrt_hit* o = &c->hits[i];
+        if (found) {
+            o->t = hit.hitT;
+            o->u = hit.u;
+            o->v = hit.v;
+            o->prim = hit.object;
+        } else {
+            o->t = IGXRT_NO_HIT;
+            o->u = o->v = 0;
+            o->prim = IGXRT_NO_RAY_HIT;
+        }
+        if (c->flags)
+            c->flags[i] = hit.events;
+    }
+}
+
+static void mixed_any_chunk(void* p, uint32_t b, uint32_t e) {
+    mixed_ctx* c = (mixed_ctx*)p;
+    for (uint32_t i = b; i < e; ++i) {
+        hitstate hit;
+        hit.hitT = IGXRT_NO_HIT;
+        hit.u = hit.v = 0;
+        hit.object = 0;
+        hit.events = 0;
+        trace_mixed_one(c->d, &c->rays[i], c->prev ? c->prev[i] : IGXRT_NO_RAY_HIT, &hit);
+        c->occ[i] = hit.hitT < tmax_effective(c->rays[i].tmax) ? 1u : 0u;
+        if (c->flags)
+            c->flags[i] = hit.events;
+    }
+}
+
+void orc_trace_geometry_mixed(const igxrt_scene_desc* scene, const igxrt_ray* rays,
+                              const uint32_t* prev_hit, uint32_t nrays, igxrt_hit* out,
+                              uint32_t* flags, int threads) {
+    mixed_ctx c = {scene, rays, prev_hit, out, NULL, flags};
+    run_parallel(mixed_closest_chunk, &c, nrays, 64, threads);
+}
+
+void orc_trace_occlusion_mixed(const igxrt_scene_desc* scene, const igxrt_ray* rays,
+                               const uint32_t* prev_hit, uint32_t nrays, uint32_t* out,
+                               uint32_t* flags, int threads) {
+    mixed_ctx c = {scene, rays, prev_hit, NULL, out, flags};
+    run_parallel(mixed_any_chunk, &c, nrays, 64, threads);
+}
+
 /* unpackHalf2x16 component: exact binary16 -> binary32. */
 static float half_to_float(uint32_t h) {
     const uint32_t sign = (h >> 15) & 1u, ex = (h >> 10) & 31u, man = h & 1023u;
@@ -546,9 +742,10 @@ typedef struct {
     float tcull;
 } best_hit;
 
-/* Box cull limit: best t widened by 2^-10, kept finite so the {+inf} box of
- * an absent child is never entered. */
-static inline float cull_limit(float t) { return fminf(fmaf(t, 0x1p-10f, t), FLT_MAX); }
+/* Box cull limit: best t widened upward by 2^-10 of its magnitude (t can be
+ * negative with a negative tmin), kept finite so the {+inf} box of an absent
+ * child is never entered. */
+static inline float cull_limit(float t) { return fminf(fmaf(fabsf(t), 0x1p-10f, t), FLT_MAX); }
 
 /* Returns 1 when the record is accepted under the (t, prim) order. */
 static inline int leaf_record(const rayprep* r, const igxrt_prim_record* rec, best_hit* b,

@@ -233,3 +233,10 @@ PROTOTYPES += [
     ("igxrt_scene_create_mixed", _st, [_vp, C.POINTER(SceneDesc), C.POINTER(BuildOptions),
                                        C.POINTER(_vp)]),
 ]
+
+# refit of moved geometry (host BVH and resident scene) and scene read-back
+PROTOTYPES += [
+    ("igxrt_bvh_refit", _st, [_vp, C.POINTER(SceneDesc)]),
+    ("igxrt_scene_refit", _st, [_vp, _vp, C.POINTER(SceneDesc), _u32, _vp]),
+    ("igxrt_scene_read_bvh", _st, [_vp, _vp, _u32, _vp, _u64, _vp, _u64]),
+]

@@ -184,6 +184,34 @@ class BVH:
         if st != 0:
             raise IgxrtError(st, buf.value.decode())
 
+    def refit(self, triangles=None, spheres=None, cubes=None, planes=None) -> None:
+        """igxrt_bvh_refit: moved primitives (the counts of the build), same tree."""
+        d, keep = scene_desc(triangles, spheres, cubes, planes)
+        check(lib().igxrt_bvh_refit(self._h, C.byref(d)), what="igxrt_bvh_refit")
+
+
+def _device_desc(triangles=None, spheres=None, cubes=None, planes=None):
+    """igxrt_scene_desc over CUDA tensors: triangles (N, 12) float32 in the
+    igxrt_triangle layout (vertex, pad word, ...); spheres / planes (N, 4);
+    cubes (N, 6) float32."""
+    d = _capi.SceneDesc()
+    keep = []
+    for field, count, arr, width in (("triangles", "triangle_count", triangles, 12),
+                                     ("spheres", "sphere_count", spheres, 4),
+                                     ("cubes", "cube_count", cubes, 6),
+                                     ("planes", "plane_count", planes, 4)):
+        if arr is None:
+            setattr(d, field, None)
+            setattr(d, count, 0)
+            continue
+        if not _is_cuda_tensor(arr) or arr.dtype != torch.float32:
+            raise TypeError(f"{field}: a float32 CUDA tensor")
+        t = arr.contiguous().reshape(-1, width)
+        keep.append(t)
+        setattr(d, field, t.data_ptr() if len(t) else None)
+        setattr(d, count, len(t))
+    return d, keep
+
 
 class Scene:
     """A BVH resident in device memory, traced through its context."""
@@ -222,6 +250,37 @@ class Scene:
     def trace_occlusion(self, rays, prev_hit=None, stream=None):
         """traceOcclusion (trace.glsl:70-98) for every ray, maxDist = ray.tmax."""
         return self.ctx.trace_any(self, rays, prev_hit, stream=stream)
+
+    # Moving geometry ---------------------------------------------------------
+    def refit(self, triangles=None, spheres=None, cubes=None, planes=None, stream=None) -> None:
+        """igxrt_scene_refit: new positions (the counts of the scene's creation),
+        node boxes recomputed on the GPU.  numpy arrays are staged by the
+        library; CUDA tensors are read in place (see _device_desc)."""
+        args = (triangles, spheres, cubes, planes)
+        on_device = any(_is_cuda_tensor(a) for a in args)
+        if on_device:
+            d, keep = _device_desc(*args)
+            flags = 0
+        else:
+            d, keep = scene_desc(*args)
+            flags = TRACE_HOST_MEMORY
+        check(lib().igxrt_scene_refit(self.ctx.handle, self._h, C.byref(d), flags,
+                                      Context._stream(stream, on_device)),
+              self.ctx.handle, "igxrt_scene_refit")
+
+    def read_bvh(self, layout: int = LAYOUT_BVH2):
+        """igxrt_scene_read_bvh: (nodes, prim records) of the resident scene."""
+        nn = self.info["bvh2_nodes" if layout == LAYOUT_BVH2 else "bvh4_nodes"]
+        i = self.info
+        nrec = i["triangle_count"] + i["sphere_count"] + i["cube_count"]
+        ndt = _capi.BVH2_NODE_DTYPE if layout == LAYOUT_BVH2 else _capi.BVH4_NODE_DTYPE
+        nodes = np.zeros(nn, dtype=ndt)
+        prims = np.zeros(nrec, dtype=_capi.PRIM_RECORD_DTYPE)
+        check(lib().igxrt_scene_read_bvh(self.ctx.handle, self._h, layout,
+                                         nodes.ctypes.data if nn else None, nn,
+                                         prims.ctypes.data if nrec else None, nrec),
+              self.ctx.handle, "igxrt_scene_read_bvh")
+        return nodes, prims
 
 
 class Context:

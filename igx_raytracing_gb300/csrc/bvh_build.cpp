@@ -592,12 +592,226 @@ igxrt_status build_bvh_mixed(const igxrt_scene_desc& d, const igxrt_build_option
 }
 
 // ------------------------------------------------------------------------
+// Refit (host): new primitive positions, same topology
+// ------------------------------------------------------------------------
+
+namespace {
+
+bool slot_empty(float lo, float hi) { return lo == kInf && hi == kInf; }
+
+// Bounds of object `id` in a scene description by the builder's rule (the
+// points it bounds: triangle vertices, sphere centre -/+ |radius|, cube
+// corners); `finite` and `maxabs` cover the same points.
+Aabb object_bounds(const igxrt_scene_desc& d, uint32_t id, bool& finite, float& maxabs) {
+    const uint32_t nt = d.triangle_count, ns = d.sphere_count;
+    float v[3][3];
+    int nv;
+    if (id < nt) {
+        const igxrt_triangle& t = d.triangles[id];
+        for (int c = 0; c < 3; ++c) {
+            v[0][c] = t.p0[c];
+            v[1][c] = t.p1[c];
+            v[2][c] = t.p2[c];
+        }
+        nv = 3;
+    } else if (id < nt + ns) {
+        const float* s = d.spheres + 4 * (size_t)(id - nt);
+        const float r = std::fabs(s[3]);
+        for (int c = 0; c < 3; ++c) {
+            v[0][c] = s[c] - r;
+            v[1][c] = s[c] + r;
+        }
+        nv = 2;
+    } else {
+        const igxrt_cube& cb = d.cubes[id - nt - ns];
+        const float start[3] = {cb.xy0[0], cb.xy0[1], cb.z0_x1[0]};
+        const float end[3] = {cb.z0_x1[1], cb.yz1[0], cb.yz1[1]};
+        for (int c = 0; c < 3; ++c) {
+            v[0][c] = start[c];
+            v[1][c] = end[c];
+        }
+        nv = 2;
+    }
+    Aabb a;
+    a.reset();
+    finite = true;
+    for (int k = 0; k < nv; ++k) {
+        for (int c = 0; c < 3; ++c) {
+            finite = finite && std::isfinite(v[k][c]);
+            maxabs = std::max(maxabs, std::fabs(v[k][c]));
+        }
+        a.grow_point(v[k]);
+    }
+    return a;
+}
+
+}  // namespace
+
+igxrt_status refit_bvh(igxrt_bvh& b, const igxrt_scene_desc& d, std::string& err) {
+    if (d.triangle_count != b.tris.size() || d.sphere_count != b.spheres.size() / 4 ||
+        d.cube_count != b.cubes.size() || d.plane_count != b.planes.size() / 4) {
+        err = "refit needs the primitive counts of the build";
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    }
+    if ((d.triangle_count && !d.triangles) || (d.sphere_count && !d.spheres) ||
+        (d.cube_count && !d.cubes) || (d.plane_count && !d.planes)) {
+        err = "a primitive buffer with a non-zero count is NULL";
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    }
+    const uint32_t n = (uint32_t)b.prims.size();
+    std::vector<Aabb> bounds(n);
+    float maxabs = 0.f;
+    for (uint32_t id = 0; id < n; ++id) {
+        bool finite;
+        bounds[id] = object_bounds(d, id, finite, maxabs);
+        if (!finite) {
+            err = format("primitive %u has a non-finite coordinate", id);
+            return IGXRT_ERROR_INVALID_ARGUMENT;
+        }
+    }
+    for (uint32_t i = 0; i < d.plane_count * 4; ++i)
+        if (!std::isfinite(d.planes[i])) {
+            err = format("plane %u has a non-finite coefficient", i / 4);
+            return IGXRT_ERROR_INVALID_ARGUMENT;
+        }
+    const float pad = std::max(maxabs * 0x1p-18f, 1e-30f);
+    b.tris.assign(d.triangles, d.triangles + d.triangle_count);
+    b.spheres.assign(d.spheres, d.spheres + 4 * (size_t)d.sphere_count);
+    b.cubes.assign(d.cubes, d.cubes + d.cube_count);
+    b.planes.assign(d.planes, d.planes + 4 * (size_t)d.plane_count);
+    const uint32_t nt = d.triangle_count, ns = d.sphere_count;
+    for (auto& r : b.prims) {
+        const uint32_t id = r.prim;
+        if (id < nt) {
+            const igxrt_triangle& t = d.triangles[id];
+            for (int a = 0; a < 3; ++a) {
+                r.p0[a] = t.p0[a];
+                r.e1[a] = t.p1[a] - t.p0[a];
+                r.e2[a] = t.p2[a] - t.p0[a];
+            }
+        } else if (id < nt + ns) {
+            const float* s = d.spheres + 4 * (size_t)(id - nt);
+            for (int a = 0; a < 3; ++a)
+                r.p0[a] = s[a];
+            r.e1[0] = s[3];
+        } else {
+            const igxrt_cube& c = d.cubes[id - nt - ns];
+            const float start[3] = {c.xy0[0], c.xy0[1], c.z0_x1[0]};
+            const float end[3] = {c.z0_x1[1], c.yz1[0], c.yz1[1]};
+            for (int a = 0; a < 3; ++a) {
+                r.p0[a] = start[a];
+                r.e1[a] = end[a];
+            }
+        }
+    }
+    auto leaf_box = [&](int32_t ref) {
+        Aabb a;
+        a.reset();
+        for (uint32_t i = (uint32_t)~ref;; ++i) {
+            a.grow(bounds[b.prims[i].prim]);
+            if (b.prims[i].leaf_end)
+                break;
+        }
+        return a;
+    };
+    auto padded = [pad](const Aabb& a, float* lo, float* hi) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = a.lo[k] - pad;
+            hi[k] = a.hi[k] + pad;
+        }
+    };
+    // preorder layouts: children have larger indices, so walk backwards
+    for (size_t i = b.nodes2.size(); i-- > 0;) {
+        igxrt_bvh2_node& nd = b.nodes2[i];
+        for (int c = 0; c < 2; ++c) {
+            float* x = c ? nd.c1_x : nd.c0_x;
+            float* y = c ? nd.c1_y : nd.c0_y;
+            float* z = c ? nd.c1_z : nd.c0_z;
+            if (slot_empty(x[0], x[1]))
+                continue;
+            float lo[3], hi[3];
+            if (nd.child[c] < 0) {
+                padded(leaf_box(nd.child[c]), lo, hi);
+            } else {
+                const igxrt_bvh2_node& m = b.nodes2[nd.child[c]];
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = kInf;
+                    hi[k] = -kInf;
+                }
+                for (int g = 0; g < 2; ++g) {
+                    const float* gx = g ? m.c1_x : m.c0_x;
+                    const float* gy = g ? m.c1_y : m.c0_y;
+                    const float* gz = g ? m.c1_z : m.c0_z;
+                    if (slot_empty(gx[0], gx[1]))
+                        continue;
+                    lo[0] = std::min(lo[0], gx[0]);
+                    hi[0] = std::max(hi[0], gx[1]);
+                    lo[1] = std::min(lo[1], gy[0]);
+                    hi[1] = std::max(hi[1], gy[1]);
+                    lo[2] = std::min(lo[2], gz[0]);
+                    hi[2] = std::max(hi[2], gz[1]);
+                }
+            }
+            x[0] = lo[0];
+            x[1] = hi[0];
+            y[0] = lo[1];
+            y[1] = hi[1];
+            z[0] = lo[2];
+            z[1] = hi[2];
+        }
+    }
+    for (size_t i = b.nodes4.size(); i-- > 0;) {
+        igxrt_bvh4_node& nd = b.nodes4[i];
+        for (int c = 0; c < 4; ++c) {
+            if (slot_empty(nd.lo_x[c], nd.hi_x[c]))
+                continue;
+            float lo[3], hi[3];
+            if (nd.child[c] < 0) {
+                padded(leaf_box(nd.child[c]), lo, hi);
+            } else {
+                const igxrt_bvh4_node& m = b.nodes4[nd.child[c]];
+                for (int k = 0; k < 3; ++k) {
+                    lo[k] = kInf;
+                    hi[k] = -kInf;
+                }
+                for (int g = 0; g < 4; ++g) {
+                    if (slot_empty(m.lo_x[g], m.hi_x[g]))
+                        continue;
+                    lo[0] = std::min(lo[0], m.lo_x[g]);
+                    hi[0] = std::max(hi[0], m.hi_x[g]);
+                    lo[1] = std::min(lo[1], m.lo_y[g]);
+                    hi[1] = std::max(hi[1], m.hi_y[g]);
+                    lo[2] = std::min(lo[2], m.lo_z[g]);
+                    hi[2] = std::max(hi[2], m.hi_z[g]);
+                }
+            }
+            nd.lo_x[c] = lo[0];
+            nd.hi_x[c] = hi[0];
+            nd.lo_y[c] = lo[1];
+            nd.hi_y[c] = hi[1];
+            nd.lo_z[c] = lo[2];
+            nd.hi_z[c] = hi[2];
+        }
+    }
+    Aabb scene;
+    scene.reset();
+    for (const Aabb& a : bounds)
+        scene.grow(a);
+    b.info.pad_abs = pad;
+    for (int a = 0; a < 3; ++a) {
+        b.info.bounds[a] = n ? scene.lo[a] : 0.f;
+        b.info.bounds[3 + a] = n ? scene.hi[a] : 0.f;
+    }
+    return IGXRT_OK;
+}
+
+// ------------------------------------------------------------------------
 // Validation
 // ------------------------------------------------------------------------
 
 namespace {
 
-bool box_empty(float lo, float hi) { return lo == kInf && hi == kInf; }
+bool box_empty(float lo, float hi) { return slot_empty(lo, hi); }
 
 struct Checker {
     const igxrt_bvh& b;
@@ -882,6 +1096,22 @@ igxrt_status igxrt_bvh_build_mixed(const igxrt_scene_desc* desc, const igxrt_bui
 
 igxrt_status igxrt_bvh_destroy(igxrt_bvh* bvh) {
     delete bvh;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_bvh_refit(igxrt_bvh* bvh, const igxrt_scene_desc* desc) {
+    if (!bvh || !desc)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    std::string err;
+    try {
+        igxrt_bvh next = *bvh;  // all or nothing: a rejected description changes nothing
+        const igxrt_status st = refit_bvh(next, *desc, err);
+        if (st != IGXRT_OK)
+            return st;
+        *bvh = std::move(next);
+    } catch (const std::bad_alloc&) {
+        return IGXRT_ERROR_OUT_OF_MEMORY;
+    }
     return IGXRT_OK;
 }
 

@@ -345,7 +345,17 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
     const size_t bp = round_up(bvh->prims.size() * sizeof(igxrt_prim_record), 256);
     const size_t bt = round_up(bvh->tris.size() * sizeof(igxrt_triangle), 256);
     const size_t bl = round_up(bvh->planes.size() * sizeof(float), 256);
-    const size_t total = std::max<size_t>(b2 + b4 + bp + bt + bl, 256);
+    std::vector<uint32_t> par2, par4;
+    try {
+        node_parents(*bvh, par2, par4);
+    } catch (const std::bad_alloc&) {
+        delete s;
+        return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "parent links");
+    }
+    const size_t nn = par2.size() + par4.size();
+    const size_t bpar = round_up(nn * sizeof(uint32_t), 256);
+    const size_t bw = round_up((kRefitStateWords + nn) * sizeof(uint32_t), 256);
+    const size_t total = b2 + b4 + bp + bt + bl + bpar + bw;
     cudaError_t e = cudaMalloc(&s->d_mem, total);
     if (e != cudaSuccess) {
         delete s;
@@ -362,7 +372,16 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
     s->planes = (const float*)(base + b2 + b4 + bp + bt);
     s->plane_count = (uint32_t)(bvh->planes.size() / 4);
     s->plane_base = (uint32_t)(bvh->tris.size() + bvh->spheres.size() / 4 + bvh->cubes.size());
-    if (!bvh->planes.empty())
+    uint32_t* parents = (uint32_t*)(base + b2 + b4 + bp + bt + bl);
+    s->parents[IGXRT_LAYOUT_BVH2] = parents;
+    s->parents[IGXRT_LAYOUT_BVH4] = parents + par2.size();
+    s->refit_words = (uint32_t*)(base + b2 + b4 + bp + bt + bl + bpar);
+    if (!par2.empty())
+        e = cudaMemcpy(parents, par2.data(), par2.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !par4.empty())
+        e = cudaMemcpy(parents + par2.size(), par4.data(), par4.size() * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !bvh->planes.empty())
         e = cudaMemcpy(base + b2 + b4 + bp + bt, bvh->planes.data(), bvh->planes.size() * sizeof(float),
                        cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !bvh->nodes2.empty())

@@ -46,11 +46,23 @@ struct igxrt_scene {
     const float* planes = nullptr;  // 4 floats per plane
     uint32_t plane_count = 0;
     uint32_t plane_base = 0;        // object id of the first plane
+    // refit: the parent of every node per layout (kNoParent at the root), and
+    // kRefitStateWords state words followed by one arrival counter per node
+    // of BVH2, then of BVH4 (zeroed before each refit)
+    const uint32_t* parents[IGXRT_LAYOUT_COUNT] = {nullptr, nullptr};
+    uint32_t* refit_words = nullptr;
 };
 
 namespace igxrt {
 
 constexpr uint32_t kQueueSlots = 4096;
+constexpr uint32_t kNoParent = 0xffffffffu;
+constexpr uint32_t kRefitStateWords = 8;
+
+// Parent links of both layouts, computed on the host at scene creation and
+// stored after the scene's other buffers (see refit.cu).
+void node_parents(const igxrt_bvh& bvh, std::vector<uint32_t>& parents2,
+                  std::vector<uint32_t>& parents4);
 
 // One traversal launch over `count` rays of one scene (device pointers).
 struct TraceRequest {

@@ -42,6 +42,10 @@ igxrt_status build_bvh(const igxrt_triangle* tris, uint32_t count,
 igxrt_status build_bvh_mixed(const igxrt_scene_desc& d, const igxrt_build_options* opts,
                              igxrt_bvh& out, std::string& err);
 
+// New primitive positions for a built tree: same topology and record order,
+// every box recomputed with the builder's padding rule (host only).
+igxrt_status refit_bvh(igxrt_bvh& bvh, const igxrt_scene_desc& d, std::string& err);
+
 // Structural validation; returns IGXRT_OK or IGXRT_ERROR_INVALID_BVH with msg.
 igxrt_status validate_bvh(const igxrt_bvh& bvh, std::string& msg);
 

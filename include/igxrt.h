@@ -233,6 +233,12 @@ igxrt_status igxrt_bvh_get_data(const igxrt_bvh* bvh, uint32_t layout,
 /* Checks structure and boxes: every triangle in exactly one leaf, every child
  * box contains its subtree, node indices in range, depth within the limit. */
 igxrt_status igxrt_bvh_validate(const igxrt_bvh* bvh, char* msg, size_t msg_len);
+/* Moves the primitives of a built BVH (same counts as at the build: an
+ * animated frame) and recomputes the primitive records and every node box,
+ * keeping the tree topology.  The boxes follow the builder's rule (bounds of
+ * the subtree widened by 2^-18 * max|coordinate|), so a refit BVH is exactly
+ * what the builder would emit for this topology. */
+igxrt_status igxrt_bvh_refit(igxrt_bvh* bvh, const igxrt_scene_desc* desc);
 /* Serialises a built BVH (both layouts and the triangle array) to a file and
  * loads it back, so a server can warm-start without rebuilding. */
 igxrt_status igxrt_bvh_save(const igxrt_bvh* bvh, const char* path);
@@ -265,6 +271,26 @@ igxrt_status igxrt_scene_create_mixed(igxrt_context* ctx, const igxrt_scene_desc
 igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bvh,
                                          igxrt_scene** out);
 igxrt_status igxrt_scene_destroy(igxrt_scene* scene);
+/*
+ * GPU refit for per-frame animation (the reference re-uploads moving spheres
+ * every frame, test/scene/niels_scene.cpp:61-70): new primitive buffers with
+ * the counts of the scene's creation (device pointers, or host pointers with
+ * IGXRT_TRACE_HOST_MEMORY) replace the old ones; primitive records and node
+ * boxes of both layouts are recomputed on the GPU bottom-up, the topology is
+ * kept.  The result equals igxrt_bvh_refit on the host.  The work is ordered
+ * on `stream` after what the caller queued there (e.g. the kernel that moved
+ * the geometry), and the call returns once it has finished, so the status can
+ * report a non-finite coordinate (IGXRT_ERROR_INVALID_ARGUMENT; the scene is
+ * then left unchanged) and igxrt_scene_get_info sees the new bounds.  Traces
+ * of the scene must not overlap the refit on another stream.
+ */
+igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igxrt_scene_desc* desc,
+                               uint32_t flags, void* stream);
+/* Copies a resident scene's nodes of `layout` and its primitive records to
+ * host arrays (sizes from igxrt_scene_get_info; synchronous). */
+igxrt_status igxrt_scene_read_bvh(igxrt_context* ctx, const igxrt_scene* scene, uint32_t layout,
+                                  void* nodes, uint64_t node_count, igxrt_prim_record* prims,
+                                  uint64_t prim_count);
 igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info);
 
 /* ---- Ray queries --------------------------------------------------------- */

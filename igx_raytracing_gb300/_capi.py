@@ -239,4 +239,7 @@ PROTOTYPES += [
     ("igxrt_bvh_refit", _st, [_vp, C.POINTER(SceneDesc)]),
     ("igxrt_scene_refit", _st, [_vp, _vp, C.POINTER(SceneDesc), _u32, _vp]),
     ("igxrt_scene_read_bvh", _st, [_vp, _vp, _u32, _vp, _u64, _vp, _u64]),
+    ("igxrt_scene_create_gpu", _st, [_vp, C.POINTER(SceneDesc), C.POINTER(BuildOptions), _u32, _vp,
+                                     C.POINTER(_vp)]),
+    ("igxrt_scene_download", _st, [_vp, _vp, C.POINTER(_vp)]),
 ]

@@ -268,6 +268,13 @@ class Scene:
                                       Context._stream(stream, on_device)),
               self.ctx.handle, "igxrt_scene_refit")
 
+    def download(self) -> BVH:
+        """igxrt_scene_download: the resident tree as a validated host BVH."""
+        h = C.c_void_p()
+        check(lib().igxrt_scene_download(self.ctx.handle, self._h, C.byref(h)), self.ctx.handle,
+              "igxrt_scene_download")
+        return BVH(h.value)
+
     def read_bvh(self, layout: int = LAYOUT_BVH2):
         """igxrt_scene_read_bvh: (nodes, prim records) of the resident scene."""
         nn = self.info["bvh2_nodes" if layout == LAYOUT_BVH2 else "bvh4_nodes"]
@@ -353,6 +360,27 @@ class Context:
         o = _build_options(**opts)
         check(lib().igxrt_scene_create_mixed(self._h, C.byref(d), C.byref(o), C.byref(h)),
               self._h, "igxrt_scene_create_mixed")
+        return Scene(self, h.value, d.triangle_count)
+
+    def create_scene_gpu(self, triangles=None, spheres=None, cubes=None, planes=None,
+                         max_leaf_size: int = 0, stream=None) -> Scene:
+        """igxrt_scene_create_gpu: the BVH built on the GPU (linear BVH).
+        numpy arrays are staged by the library; CUDA tensors are read in place
+        (triangles (N, 12) float32 in the igxrt_triangle layout, spheres /
+        planes (N, 4), cubes (N, 6))."""
+        args = (triangles, spheres, cubes, planes)
+        on_device = any(_is_cuda_tensor(a) for a in args)
+        if on_device:
+            d, keep = _device_desc(*args)
+            flags = 0
+        else:
+            d, keep = scene_desc(*args)
+            flags = TRACE_HOST_MEMORY
+        h = C.c_void_p()
+        o = _build_options(max_leaf_size=max_leaf_size)
+        check(lib().igxrt_scene_create_gpu(self._h, C.byref(d), C.byref(o), flags,
+                                           Context._stream(stream, on_device), C.byref(h)),
+              self._h, "igxrt_scene_create_gpu")
         return Scene(self, h.value, d.triangle_count)
 
     # -- queries -----------------------------------------------------------

@@ -720,8 +720,37 @@ igxrt_status refit_bvh(igxrt_bvh& b, const igxrt_scene_desc& d, std::string& err
             hi[k] = a.hi[k] + pad;
         }
     };
-    // preorder layouts: children have larger indices, so walk backwards
-    for (size_t i = b.nodes2.size(); i-- > 0;) {
+    // children before parents: reversed depth-first order from the root (the
+    // host builder's arrays are preorder already, GPU-built ones are not)
+    auto bottom_up = [](size_t count, auto&& kids) {
+        std::vector<uint32_t> order, stack;
+        order.reserve(count);
+        if (count)
+            stack.push_back(0);
+        while (!stack.empty() && order.size() < count) {
+            const uint32_t i = stack.back();
+            stack.pop_back();
+            order.push_back(i);
+            kids(i, stack);
+        }
+        std::reverse(order.begin(), order.end());
+        return order;
+    };
+    const std::vector<uint32_t> order2 = bottom_up(b.nodes2.size(), [&](uint32_t i, std::vector<uint32_t>& st) {
+        const igxrt_bvh2_node& nd = b.nodes2[i];
+        for (int c = 0; c < 2; ++c) {
+            const float* x = c ? nd.c1_x : nd.c0_x;
+            if (!slot_empty(x[0], x[1]) && nd.child[c] >= 0 && (size_t)nd.child[c] < b.nodes2.size())
+                st.push_back((uint32_t)nd.child[c]);
+        }
+    });
+    const std::vector<uint32_t> order4 = bottom_up(b.nodes4.size(), [&](uint32_t i, std::vector<uint32_t>& st) {
+        const igxrt_bvh4_node& nd = b.nodes4[i];
+        for (int c = 0; c < 4; ++c)
+            if (!slot_empty(nd.lo_x[c], nd.hi_x[c]) && nd.child[c] >= 0 && (size_t)nd.child[c] < b.nodes4.size())
+                st.push_back((uint32_t)nd.child[c]);
+    });
+    for (const uint32_t i : order2) {
         igxrt_bvh2_node& nd = b.nodes2[i];
         for (int c = 0; c < 2; ++c) {
             float* x = c ? nd.c1_x : nd.c0_x;
@@ -760,7 +789,7 @@ igxrt_status refit_bvh(igxrt_bvh& b, const igxrt_scene_desc& d, std::string& err
             z[1] = hi[2];
         }
     }
-    for (size_t i = b.nodes4.size(); i-- > 0;) {
+    for (const uint32_t i : order4) {
         igxrt_bvh4_node& nd = b.nodes4[i];
         for (int c = 0; c < 4; ++c) {
             if (slot_empty(nd.lo_x[c], nd.hi_x[c]))

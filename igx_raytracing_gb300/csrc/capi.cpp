@@ -73,6 +73,51 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
     return IGXRT_OK;
 }
 
+// One device allocation per scene, 256-byte aligned sub-buffers in this
+// order: BVH2 nodes, BVH4 nodes, records, triangles, planes, parent links of
+// both layouts, refit words.  Fills every pointer and count of the scene from
+// `info` and the node counts; the contents are the caller's to write.
+igxrt_status allocate_scene(igxrt_context* ctx, const igxrt_bvh_info& info, uint32_t n2, uint32_t n4,
+                            igxrt_scene*& out) {
+    out = nullptr;
+    igxrt_scene* s = new (std::nothrow) igxrt_scene();
+    if (!s)
+        return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "scene object");
+    s->device = ctx->device;
+    s->info = info;
+    const size_t records = (size_t)info.triangle_count + info.sphere_count + info.cube_count;
+    const size_t b2 = round_up((size_t)n2 * sizeof(igxrt_bvh2_node), 256);
+    const size_t b4 = round_up((size_t)n4 * sizeof(igxrt_bvh4_node), 256);
+    const size_t bp = round_up(records * sizeof(igxrt_prim_record), 256);
+    const size_t bt = round_up((size_t)info.triangle_count * sizeof(igxrt_triangle), 256);
+    const size_t bl = round_up((size_t)info.plane_count * 16, 256);
+    const size_t nn = (size_t)n2 + n4;
+    const size_t bpar = round_up(nn * sizeof(uint32_t), 256);
+    const size_t bw = round_up((kRefitStateWords + nn) * sizeof(uint32_t), 256);
+    cudaError_t e = cudaMalloc(&s->d_mem, b2 + b4 + bp + bt + bl + bpar + bw);
+    if (e != cudaSuccess) {
+        delete s;
+        return cuda_fail(ctx, e, "scene allocation");
+    }
+    char* base = (char*)s->d_mem;
+    s->nodes[IGXRT_LAYOUT_BVH2] = base;
+    s->nodes[IGXRT_LAYOUT_BVH4] = base + b2;
+    s->prims = (const igxrt_prim_record*)(base + b2 + b4);
+    s->tris = (const igxrt_triangle*)(base + b2 + b4 + bp);
+    s->planes = (const float*)(base + b2 + b4 + bp + bt);
+    uint32_t* parents = (uint32_t*)(base + b2 + b4 + bp + bt + bl);
+    s->parents[IGXRT_LAYOUT_BVH2] = parents;
+    s->parents[IGXRT_LAYOUT_BVH4] = parents + n2;
+    s->refit_words = (uint32_t*)(base + b2 + b4 + bp + bt + bl + bpar);
+    s->node_count[IGXRT_LAYOUT_BVH2] = n2;
+    s->node_count[IGXRT_LAYOUT_BVH4] = n4;
+    s->mixed = info.sphere_count || info.cube_count || info.plane_count;
+    s->plane_count = info.plane_count;
+    s->plane_base = (uint32_t)records;
+    out = s;
+    return IGXRT_OK;
+}
+
 }  // namespace igxrt
 
 using namespace igxrt;
@@ -144,8 +189,6 @@ igxrt_status igxrt::read_status(igxrt_context* ctx) {
 }
 
 namespace {
-
-size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_ray* rays,
                           const uint32_t* prev, uint32_t count, uint32_t mode, void* out,
@@ -335,66 +378,31 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
     DeviceGuard guard(ctx->device);
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
-    igxrt_scene* s = new (std::nothrow) igxrt_scene();
-    if (!s)
-        return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "scene object");
-    s->device = ctx->device;
-    s->info = bvh->info;
-    const size_t b2 = round_up(bvh->nodes2.size() * sizeof(igxrt_bvh2_node), 256);
-    const size_t b4 = round_up(bvh->nodes4.size() * sizeof(igxrt_bvh4_node), 256);
-    const size_t bp = round_up(bvh->prims.size() * sizeof(igxrt_prim_record), 256);
-    const size_t bt = round_up(bvh->tris.size() * sizeof(igxrt_triangle), 256);
-    const size_t bl = round_up(bvh->planes.size() * sizeof(float), 256);
     std::vector<uint32_t> par2, par4;
     try {
         node_parents(*bvh, par2, par4);
     } catch (const std::bad_alloc&) {
-        delete s;
         return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "parent links");
     }
-    const size_t nn = par2.size() + par4.size();
-    const size_t bpar = round_up(nn * sizeof(uint32_t), 256);
-    const size_t bw = round_up((kRefitStateWords + nn) * sizeof(uint32_t), 256);
-    const size_t total = b2 + b4 + bp + bt + bl + bpar + bw;
-    cudaError_t e = cudaMalloc(&s->d_mem, total);
+    igxrt_scene* s = nullptr;
+    igxrt_status st = allocate_scene(ctx, bvh->info, (uint32_t)bvh->nodes2.size(),
+                                     (uint32_t)bvh->nodes4.size(), s);
+    if (st != IGXRT_OK)
+        return st;
+    cudaError_t e = cudaSuccess;
+    auto up = [&e](const void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes)
+            e = cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
+    };
+    up(s->parents[IGXRT_LAYOUT_BVH2], par2.data(), par2.size() * sizeof(uint32_t));
+    up(s->parents[IGXRT_LAYOUT_BVH4], par4.data(), par4.size() * sizeof(uint32_t));
+    up(s->planes, bvh->planes.data(), bvh->planes.size() * sizeof(float));
+    up(s->nodes[IGXRT_LAYOUT_BVH2], bvh->nodes2.data(), bvh->nodes2.size() * sizeof(igxrt_bvh2_node));
+    up(s->nodes[IGXRT_LAYOUT_BVH4], bvh->nodes4.data(), bvh->nodes4.size() * sizeof(igxrt_bvh4_node));
+    up(s->prims, bvh->prims.data(), bvh->prims.size() * sizeof(igxrt_prim_record));
+    up(s->tris, bvh->tris.data(), bvh->tris.size() * sizeof(igxrt_triangle));
     if (e != cudaSuccess) {
-        delete s;
-        return cuda_fail(ctx, e, "scene allocation");
-    }
-    char* base = (char*)s->d_mem;
-    s->nodes[IGXRT_LAYOUT_BVH2] = base;
-    s->nodes[IGXRT_LAYOUT_BVH4] = base + b2;
-    s->prims = (const igxrt_prim_record*)(base + b2 + b4);
-    s->tris = (const igxrt_triangle*)(base + b2 + b4 + bp);
-    s->node_count[IGXRT_LAYOUT_BVH2] = (uint32_t)bvh->nodes2.size();
-    s->node_count[IGXRT_LAYOUT_BVH4] = (uint32_t)bvh->nodes4.size();
-    s->mixed = !bvh->spheres.empty() || !bvh->cubes.empty() || !bvh->planes.empty();
-    s->planes = (const float*)(base + b2 + b4 + bp + bt);
-    s->plane_count = (uint32_t)(bvh->planes.size() / 4);
-    s->plane_base = (uint32_t)(bvh->tris.size() + bvh->spheres.size() / 4 + bvh->cubes.size());
-    uint32_t* parents = (uint32_t*)(base + b2 + b4 + bp + bt + bl);
-    s->parents[IGXRT_LAYOUT_BVH2] = parents;
-    s->parents[IGXRT_LAYOUT_BVH4] = parents + par2.size();
-    s->refit_words = (uint32_t*)(base + b2 + b4 + bp + bt + bl + bpar);
-    if (!par2.empty())
-        e = cudaMemcpy(parents, par2.data(), par2.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !par4.empty())
-        e = cudaMemcpy(parents + par2.size(), par4.data(), par4.size() * sizeof(uint32_t),
-                       cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !bvh->planes.empty())
-        e = cudaMemcpy(base + b2 + b4 + bp + bt, bvh->planes.data(), bvh->planes.size() * sizeof(float),
-                       cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !bvh->nodes2.empty())
-        e = cudaMemcpy(base, bvh->nodes2.data(), bvh->nodes2.size() * sizeof(igxrt_bvh2_node), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !bvh->nodes4.empty())
-        e = cudaMemcpy(base + b2, bvh->nodes4.data(), bvh->nodes4.size() * sizeof(igxrt_bvh4_node), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !bvh->prims.empty())
-        e = cudaMemcpy(base + b2 + b4, bvh->prims.data(), bvh->prims.size() * sizeof(igxrt_prim_record), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !bvh->tris.empty())
-        e = cudaMemcpy(base + b2 + b4 + bp, bvh->tris.data(), bvh->tris.size() * sizeof(igxrt_triangle), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-        cudaFree(s->d_mem);
-        delete s;
+        igxrt_scene_destroy(s);
         return cuda_fail(ctx, e, "scene upload");
     }
     *out = s;
@@ -455,6 +463,79 @@ igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info
     if (!scene || !info)
         return IGXRT_ERROR_INVALID_ARGUMENT;
     *info = scene->info;
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_scene_download(igxrt_context* ctx, const igxrt_scene* scene, igxrt_bvh** out) {
+    if (!ctx || !out)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    igxrt_status st = check_scene(ctx, scene);
+    if (st != IGXRT_OK)
+        return st;
+    DeviceGuard guard(ctx->device);
+    if (!guard.ok())
+        return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
+    igxrt_bvh* b = new (std::nothrow) igxrt_bvh();
+    if (!b)
+        return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "BVH object");
+    const igxrt_bvh_info& info = scene->info;
+    const size_t records = (size_t)info.triangle_count + info.sphere_count + info.cube_count;
+    cudaError_t e = cudaSuccess;
+    try {
+        b->info = info;
+        b->nodes2.resize(scene->node_count[IGXRT_LAYOUT_BVH2]);
+        b->nodes4.resize(scene->node_count[IGXRT_LAYOUT_BVH4]);
+        b->prims.resize(records);
+        b->tris.resize(info.triangle_count);
+        b->planes.resize(4 * (size_t)info.plane_count);
+        b->spheres.resize(4 * (size_t)info.sphere_count);
+        b->cubes.resize(info.cube_count);
+    } catch (const std::bad_alloc&) {
+        delete b;
+        return fail(ctx, IGXRT_ERROR_OUT_OF_MEMORY, "host memory for the BVH");
+    }
+    e = cudaDeviceSynchronize();
+    auto down = [&e](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes)
+            e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+    };
+    down(b->nodes2.data(), scene->nodes[IGXRT_LAYOUT_BVH2], b->nodes2.size() * sizeof(igxrt_bvh2_node));
+    down(b->nodes4.data(), scene->nodes[IGXRT_LAYOUT_BVH4], b->nodes4.size() * sizeof(igxrt_bvh4_node));
+    down(b->prims.data(), scene->prims, records * sizeof(igxrt_prim_record));
+    down(b->tris.data(), scene->tris, b->tris.size() * sizeof(igxrt_triangle));
+    down(b->planes.data(), scene->planes, b->planes.size() * sizeof(float));
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(ctx, e, "scene download");
+    }
+    // spheres and cubes live only in their records: (centre, radius), (start, end)
+    const uint32_t nt = info.triangle_count, ns = info.sphere_count;
+    for (const igxrt_prim_record& r : b->prims) {
+        if (r.prim >= records)
+            continue;  // the validator below reports it
+        if (r.prim >= nt && r.prim < nt + ns) {
+            float* s = &b->spheres[4 * (size_t)(r.prim - nt)];
+            s[0] = r.p0[0];
+            s[1] = r.p0[1];
+            s[2] = r.p0[2];
+            s[3] = r.e1[0];
+        } else if (r.prim >= nt + ns) {
+            igxrt_cube& c = b->cubes[r.prim - nt - ns];
+            c.xy0[0] = r.p0[0];
+            c.xy0[1] = r.p0[1];
+            c.z0_x1[0] = r.p0[2];
+            c.z0_x1[1] = r.e1[0];
+            c.yz1[0] = r.e1[1];
+            c.yz1[1] = r.e1[2];
+        }
+    }
+    std::string msg;
+    if ((st = validate_bvh(*b, msg)) != IGXRT_OK) {
+        delete b;
+        return fail(ctx, st, "downloaded scene: " + msg);
+    }
+    *out = b;
     return IGXRT_OK;
 }
 

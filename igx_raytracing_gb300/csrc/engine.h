@@ -59,6 +59,13 @@ constexpr uint32_t kQueueSlots = 4096;
 constexpr uint32_t kNoParent = 0xffffffffu;
 constexpr uint32_t kRefitStateWords = 8;
 
+inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// One device allocation for a scene of `info`'s primitive counts and n2 / n4
+// nodes; every pointer of the scene is set, the contents are unwritten.
+igxrt_status allocate_scene(igxrt_context* ctx, const igxrt_bvh_info& info, uint32_t n2, uint32_t n4,
+                            igxrt_scene*& out);
+
 // Parent links of both layouts, computed on the host at scene creation and
 // stored after the scene's other buffers (see refit.cu).
 void node_parents(const igxrt_bvh& bvh, std::vector<uint32_t>& parents2,

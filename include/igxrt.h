@@ -15,7 +15,8 @@
  *       submodule, which the reference checkout leaves empty).
  *
  * The reference loops linearly over every primitive; this engine builds a BVH
- * on the host and traverses it with CUDA kernels for sm_103a.  The result of
+ * (on the host, or on the GPU for per-frame geometry) and traverses it with
+ * CUDA kernels for sm_103a.  The result of
  * every query equals the linear loop's: the closest hit is the smallest t
  * accepted by the reference's triangle test (res/shaders/primitive.glsl:239-284),
  * ties going to the lowest primitive index (the loop runs in index order and
@@ -29,8 +30,9 @@
  *   - Trace calls are ordered on the CUDA stream passed as `stream`
  *     (a cudaStream_t cast to void*; NULL = the legacy default stream).
  *     Without IGXRT_TRACE_HOST_MEMORY they return as soon as the work is queued.
- *   - A context is used by one host thread at a time.  Scenes are immutable
- *     after creation and may be traced from any context on the same device.
+ *   - A context is used by one host thread at a time.  Scenes change only
+ *     through igxrt_scene_refit and may be traced from any context on the
+ *     same device.
  */
 #ifndef IGXRT_H
 #define IGXRT_H
@@ -270,6 +272,21 @@ igxrt_status igxrt_scene_create_mixed(igxrt_context* ctx, const igxrt_scene_desc
 /* Uploads an already built BVH. */
 igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bvh,
                                          igxrt_scene** out);
+/*
+ * Builds the BVH on the GPU (a linear BVH: Morton order and radix tree) for
+ * geometry that changes every frame; no reference counterpart (the reference
+ * re-uploads its scene per frame, test/scene/niels_scene.cpp:61-70, and has no
+ * acceleration structure).  Same node formats, records, padding rule and
+ * query results as igxrt_scene_create_mixed; the tree differs (Morton splits,
+ * not SAH), so traversal visits more nodes.  Primitive buffers are device
+ * pointers, or host pointers with IGXRT_TRACE_HOST_MEMORY.  opts: only
+ * max_leaf_size is used (0 = 4): a subtree of at most that many objects
+ * becomes one leaf.  The work is ordered on `stream`; the call returns once
+ * the scene is ready.
+ */
+igxrt_status igxrt_scene_create_gpu(igxrt_context* ctx, const igxrt_scene_desc* desc,
+                                    const igxrt_build_options* opts, uint32_t flags, void* stream,
+                                    igxrt_scene** out);
 igxrt_status igxrt_scene_destroy(igxrt_scene* scene);
 /*
  * GPU refit for per-frame animation (the reference re-uploads moving spheres
@@ -286,6 +303,10 @@ igxrt_status igxrt_scene_destroy(igxrt_scene* scene);
  */
 igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igxrt_scene_desc* desc,
                                uint32_t flags, void* stream);
+/* Copies a resident scene (both layouts, records, primitive buffers, info)
+ * into a new host BVH and validates it, e.g. to save a GPU-built or refit
+ * tree for a warm start (synchronous; free with igxrt_bvh_destroy). */
+igxrt_status igxrt_scene_download(igxrt_context* ctx, const igxrt_scene* scene, igxrt_bvh** out);
 /* Copies a resident scene's nodes of `layout` and its primitive records to
  * host arrays (sizes from igxrt_scene_get_info; synchronous). */
 igxrt_status igxrt_scene_read_bvh(igxrt_context* ctx, const igxrt_scene* scene, uint32_t layout,

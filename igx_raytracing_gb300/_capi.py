@@ -19,7 +19,8 @@ NO_RAY_HIT = 0xFFFFFFFF
 
 LAYOUT_BVH2 = 0
 LAYOUT_BVH4 = 1
-LAYOUT_COUNT = 2
+LAYOUT_BVH8 = 2
+LAYOUT_COUNT = 3
 TRACE_HOST_MEMORY = 1
 STATIC_SCRATCH_BYTES = 16 << 20
 STATIC_MAX_RAYS = 320000
@@ -51,7 +52,13 @@ BVH2_NODE_DTYPE = np.dtype([("c0_x", "<f4", (2,)), ("c0_y", "<f4", (2,)), ("c1_x
 BVH4_NODE_DTYPE = np.dtype([("lo_x", "<f4", (4,)), ("hi_x", "<f4", (4,)), ("lo_y", "<f4", (4,)),
                             ("hi_y", "<f4", (4,)), ("lo_z", "<f4", (4,)), ("hi_z", "<f4", (4,)),
                             ("child", "<i4", (4,)), ("pad", "<u4", (4,))])
+BVH8_NODE_DTYPE = np.dtype([("origin", "<f4", (3,)), ("exp", "i1", (3,)), ("valid", "u1"),
+                            ("lo_x", "u1", (8,)), ("hi_x", "u1", (8,)), ("lo_y", "u1", (8,)),
+                            ("hi_y", "u1", (8,)), ("lo_z", "u1", (8,)), ("hi_z", "u1", (8,)),
+                            ("child", "<i4", (8,))])
+NODE_DTYPES = {LAYOUT_BVH2: BVH2_NODE_DTYPE, LAYOUT_BVH4: BVH4_NODE_DTYPE, LAYOUT_BVH8: BVH8_NODE_DTYPE}
 assert TRIANGLE_DTYPE.itemsize == 48 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.itemsize == 16
+assert BVH8_NODE_DTYPE.itemsize == 96
 assert PRIM_RECORD_DTYPE.itemsize == 48 and BVH2_NODE_DTYPE.itemsize == 64
 assert BVH4_NODE_DTYPE.itemsize == 128
 
@@ -66,7 +73,7 @@ class BvhInfo(C.Structure):
                 ("bvh4_nodes", C.c_uint32), ("leaf_count", C.c_uint32), ("max_depth", C.c_uint32),
                 ("max_leaf_size", C.c_uint32), ("sah_cost", C.c_float), ("bounds", C.c_float * 6),
                 ("pad_abs", C.c_float), ("max_stack", C.c_uint32 * LAYOUT_COUNT),
-                ("device_bytes", C.c_uint64), ("sphere_count", C.c_uint32),
+                ("bvh8_nodes", C.c_uint32), ("device_bytes", C.c_uint64), ("sphere_count", C.c_uint32),
                 ("cube_count", C.c_uint32), ("plane_count", C.c_uint32), ("reserved", C.c_uint32)]
 
 

@@ -22,7 +22,7 @@ from typing import Optional
 import numpy as np
 
 from . import _capi
-from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, RAY_DTYPE, TRACE_HOST_MEMORY,
+from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, RAY_DTYPE, TRACE_HOST_MEMORY,
                     TRIANGLE_DTYPE, BuildOptions, BvhInfo, IgxrtError, LaunchParams, check, lib)
 
 try:  # torch is only needed for device-memory calls
@@ -80,7 +80,7 @@ def _build_options(max_leaf_size=0, sah_bins=0, node_cost=0.0, tri_cost=0.0, thr
 def _info_dict(info: BvhInfo) -> dict:
     return {
         "triangle_count": info.triangle_count, "bvh2_nodes": info.bvh2_nodes,
-        "bvh4_nodes": info.bvh4_nodes, "leaf_count": info.leaf_count,
+        "bvh4_nodes": info.bvh4_nodes, "bvh8_nodes": info.bvh8_nodes, "leaf_count": info.leaf_count,
         "max_depth": info.max_depth, "max_leaf_size": info.max_leaf_size,
         "sah_cost": info.sah_cost, "bounds": list(info.bounds), "pad_abs": info.pad_abs,
         "max_stack": list(info.max_stack), "device_bytes": info.device_bytes,
@@ -169,7 +169,7 @@ class BVH:
         nodes, nn, prims, np_ = C.c_void_p(), C.c_uint64(), C.c_void_p(), C.c_uint64()
         check(lib().igxrt_bvh_get_data(self._h, layout, C.byref(nodes), C.byref(nn),
                                        C.byref(prims), C.byref(np_)))
-        ndt = _capi.BVH2_NODE_DTYPE if layout == LAYOUT_BVH2 else _capi.BVH4_NODE_DTYPE
+        ndt = _capi.NODE_DTYPES[layout]
         node_arr = np.zeros(nn.value, dtype=ndt)
         prim_arr = np.zeros(np_.value, dtype=_capi.PRIM_RECORD_DTYPE)
         if nn.value:
@@ -277,10 +277,10 @@ class Scene:
 
     def read_bvh(self, layout: int = LAYOUT_BVH2):
         """igxrt_scene_read_bvh: (nodes, prim records) of the resident scene."""
-        nn = self.info["bvh2_nodes" if layout == LAYOUT_BVH2 else "bvh4_nodes"]
         i = self.info
+        nn = i[("bvh2_nodes", "bvh4_nodes", "bvh8_nodes")[layout]]
         nrec = i["triangle_count"] + i["sphere_count"] + i["cube_count"]
-        ndt = _capi.BVH2_NODE_DTYPE if layout == LAYOUT_BVH2 else _capi.BVH4_NODE_DTYPE
+        ndt = _capi.NODE_DTYPES[layout]
         nodes = np.zeros(nn, dtype=ndt)
         prims = np.zeros(nrec, dtype=_capi.PRIM_RECORD_DTYPE)
         check(lib().igxrt_scene_read_bvh(self.ctx.handle, self._h, layout,
@@ -635,4 +635,4 @@ class Batch:
 
 
 __all__ = ["BVH", "Batch", "Context", "Scene", "Server", "IgxrtError", "as_rays", "as_triangles",
-           "make_rays", "LAYOUT_BVH2", "LAYOUT_BVH4"]
+           "make_rays", "LAYOUT_BVH2", "LAYOUT_BVH4", "LAYOUT_BVH8"]

@@ -155,7 +155,13 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
     if (!count || !items)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "autotune needs at least one item");
     const uint32_t reps = opts && opts->reps ? opts->reps : 3;
-    const uint32_t mask = opts && opts->layouts_mask ? opts->layouts_mask : ((1u << IGXRT_LAYOUT_COUNT) - 1);
+    uint32_t mask = opts && opts->layouts_mask ? opts->layouts_mask : ((1u << IGXRT_LAYOUT_COUNT) - 1);
+    for (uint32_t i = 0; i < count; ++i)  // only layouts every scene has
+        for (uint32_t l = 0; l < IGXRT_LAYOUT_COUNT; ++l)
+            if (items[i].scene && !items[i].scene->has_layout(l))
+                mask &= ~(1u << l);
+    if (!(mask & ((1u << IGXRT_LAYOUT_COUNT) - 1)))
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "autotune: no node layout common to all scenes");
     const std::string key = ctx->device_name + "|" +
                             ((opts && opts->class_key) ? std::string(opts->class_key) : derive_key(items, count));
     const char* cache = opts ? opts->cache_path : nullptr;
@@ -194,7 +200,7 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
     if (cur_ms < 0)
         return fail(ctx, IGXRT_ERROR_CUDA, "autotune: the starting parameters do not launch");
 
-    const std::vector<uint32_t> layouts = {IGXRT_LAYOUT_BVH2, IGXRT_LAYOUT_BVH4};
+    const std::vector<uint32_t> layouts = {IGXRT_LAYOUT_BVH2, IGXRT_LAYOUT_BVH4, IGXRT_LAYOUT_BVH8};
     const std::vector<uint32_t> packets = {32, 64, 128, 256};
     const std::vector<uint32_t> refills = {1, 2, 4, 8, 16};
     const std::vector<uint32_t> blocks = {64, 128, 256};

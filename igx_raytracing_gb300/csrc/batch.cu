@@ -146,6 +146,8 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
 using BatchFn = void (*)(BatchArgs);
 
 static BatchFn select_batch_kernel(uint32_t layout) {
+    if (layout == IGXRT_LAYOUT_BVH8)
+        return batch_kernel<IGXRT_LAYOUT_BVH8>;
     return layout == IGXRT_LAYOUT_BVH4 ? batch_kernel<IGXRT_LAYOUT_BVH4> : batch_kernel<IGXRT_LAYOUT_BVH2>;
 }
 
@@ -172,6 +174,8 @@ igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items
         if (it.scene->mixed)
             return fail(ctx, IGXRT_ERROR_UNSUPPORTED,
                         format("item %u: batches take triangle-only scenes", i));
+        if (!it.scene->has_layout(p.layout))
+            return fail(ctx, IGXRT_ERROR_UNSUPPORTED, format("item %u: the scene has no layout %u", i, p.layout));
         if (it.mode > 1)
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: unknown mode %u", i, it.mode));
         if (it.count && (!it.rays || !it.out))

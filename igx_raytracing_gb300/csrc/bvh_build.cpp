@@ -40,6 +40,9 @@ namespace {
 
 constexpr float kInf = INFINITY;
 
+// The {+inf, +inf} slab of an absent child.
+bool slot_empty(float lo, float hi) { return lo == kInf && hi == kInf; }
+
 struct Aabb {
     float lo[3], hi[3];
     void reset() {
@@ -394,6 +397,110 @@ uint32_t stack_bound2(const std::vector<igxrt_bvh2_node>& n, int32_t i) {
     return deepest + (e1 ? 0u : 1u);
 }
 
+uint32_t stack_bound8(const std::vector<igxrt_bvh8_node>& n, int32_t i) {
+    const igxrt_bvh8_node& x = n[i];
+    uint32_t deepest = 0, used = 0;
+    for (int c = 0; c < 8; ++c) {
+        if (!(x.valid >> c & 1))
+            continue;
+        ++used;
+        if (x.child[c] >= 0)
+            deepest = std::max(deepest, stack_bound8(n, x.child[c]));
+    }
+    return deepest + (used ? used - 1 : 0);
+}
+
+// BVH8 from the BVH2 arrays: a node takes its BVH2 node's slots and opens the
+// interior slot of largest area until eight slots are used; interior slots
+// become BVH8 nodes (preorder), leaf slots keep their record ranges.  Every
+// slot remembers its BVH2 source so the refit can re-quantize it.
+struct Bvh8Emitter {
+    igxrt_bvh& b;
+
+    static float slot_area(const igxrt_bvh2_node& m, int c) {
+        const float* x = c ? m.c1_x : m.c0_x;
+        const float* y = c ? m.c1_y : m.c0_y;
+        const float* z = c ? m.c1_z : m.c0_z;
+        const float dx = x[1] - x[0], dy = y[1] - y[0], dz = z[1] - z[0];
+        return dx * dy + dy * dz + dz * dx;
+    }
+
+    uint32_t emit(uint32_t node2) {
+        struct Kid {
+            int32_t ref;
+            uint32_t src;
+            float area;
+        };
+        Kid kids[8];
+        int used = 0;
+        auto add_slots = [&](uint32_t k, int at) {
+            const igxrt_bvh2_node& m = b.nodes2[k];
+            Kid got[2];
+            int n = 0;
+            for (int c = 0; c < 2; ++c) {
+                const float* x = c ? m.c1_x : m.c0_x;
+                if (slot_empty(x[0], x[1]))
+                    continue;
+                got[n++] = Kid{m.child[c], 2 * k + (uint32_t)c, slot_area(m, c)};
+            }
+            // replace kids[at] (or append when at == used) by the n slots
+            const int tail = at < used ? at + 1 : used;
+            for (int s = used - 1; s >= tail; --s)
+                kids[s + n - (at < used ? 1 : 0)] = kids[s];
+            for (int s = 0; s < n; ++s)
+                kids[at + s] = got[s];
+            used += n - (at < used ? 1 : 0);
+        };
+        add_slots(node2, 0);
+        while (used < 8) {
+            int pick = -1;
+            float best = -1.f;
+            for (int s = 0; s < used; ++s)
+                if (kids[s].ref >= 0 && kids[s].area > best) {
+                    best = kids[s].area;
+                    pick = s;
+                }
+            if (pick < 0)
+                break;
+            add_slots((uint32_t)kids[pick].ref, pick);
+        }
+        const uint32_t idx = (uint32_t)b.nodes8.size();
+        b.nodes8.push_back(igxrt_bvh8_node{});
+        b.src8.resize(b.src8.size() + 8, kNoSource);
+        int32_t child[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int s = 0; s < used; ++s)
+            child[s] = kids[s].ref >= 0 ? (int32_t)emit((uint32_t)kids[s].ref) : kids[s].ref;
+        igxrt_bvh8_node& o = b.nodes8[idx];
+        for (int s = 0; s < used; ++s) {
+            o.valid |= (uint8_t)(1u << s);
+            o.child[s] = child[s];
+            b.src8[8 * (size_t)idx + s] = kids[s].src;
+        }
+        bvh8_quantize_node(b.nodes2.data(), &b.src8[8 * (size_t)idx], o);
+        return idx;
+    }
+};
+
+// Adds the BVH8 layout to a built tree, or leaves it out (bvh8_nodes = 0)
+// when its traversal stack would exceed the kernels' capacity.
+void add_bvh8(igxrt_bvh& b) {
+    b.nodes8.clear();
+    b.src8.clear();
+    b.info.bvh8_nodes = 0;
+    b.info.max_stack[IGXRT_LAYOUT_BVH8] = 0;
+    if (b.nodes2.empty())
+        return;
+    Bvh8Emitter{b}.emit(0);
+    const uint32_t bound = stack_bound8(b.nodes8, 0);
+    if (bound > kStackCapacity) {
+        b.nodes8.clear();
+        b.src8.clear();
+        return;
+    }
+    b.info.bvh8_nodes = (uint32_t)b.nodes8.size();
+    b.info.max_stack[IGXRT_LAYOUT_BVH8] = bound;
+}
+
 uint32_t stack_bound4(const std::vector<igxrt_bvh4_node>& n, int32_t i) {
     const igxrt_bvh4_node& x = n[i];
     uint32_t deepest = 0, used = 0;
@@ -583,8 +690,10 @@ igxrt_status build_bvh_mixed(const igxrt_scene_desc& d, const igxrt_build_option
     info.max_stack[IGXRT_LAYOUT_BVH4] = stack_bound4(out.nodes4, 0);
     info.bvh2_nodes = (uint32_t)out.nodes2.size();
     info.bvh4_nodes = (uint32_t)out.nodes4.size();
+    add_bvh8(out);
     info.device_bytes = sizeof(igxrt_bvh2_node) * out.nodes2.size() +
                         sizeof(igxrt_bvh4_node) * out.nodes4.size() +
+                        sizeof(igxrt_bvh8_node) * out.nodes8.size() + sizeof(uint32_t) * out.src8.size() +
                         sizeof(igxrt_prim_record) * out.prims.size() +
                         sizeof(igxrt_triangle) * out.tris.size() +
                         sizeof(float) * out.planes.size();
@@ -596,8 +705,6 @@ igxrt_status build_bvh_mixed(const igxrt_scene_desc& d, const igxrt_build_option
 // ------------------------------------------------------------------------
 
 namespace {
-
-bool slot_empty(float lo, float hi) { return lo == kInf && hi == kInf; }
 
 // Bounds of object `id` in a scene description by the builder's rule (the
 // points it bounds: triangle vertices, sphere centre -/+ |radius|, cube
@@ -822,6 +929,9 @@ igxrt_status refit_bvh(igxrt_bvh& b, const igxrt_scene_desc& d, std::string& err
             nd.hi_z[c] = hi[2];
         }
     }
+    // BVH8: re-quantized from the refit BVH2 boxes of its slots
+    for (size_t i = 0; i < b.nodes8.size(); ++i)
+        bvh8_quantize_node(b.nodes2.data(), &b.src8[8 * i], b.nodes8[i]);
     Aabb scene;
     scene.reset();
     for (const Aabb& a : bounds)
@@ -908,6 +1018,59 @@ struct Checker {
             }
             if (r.leaf_end)
                 break;
+        }
+        return true;
+    }
+
+    // BVH8: every slot's decoded box (as the kernels decode it) must hold the
+    // bounds of everything below it; `content` returns those bounds.
+    bool node8(const igxrt_scene_desc& d, int32_t node, uint32_t depth, Aabb& content) {
+        if (node < 0 || (size_t)node >= b.nodes8.size())
+            return fail(format("BVH8 node index %d out of range", node));
+        if (node_seen[node])
+            return fail(format("BVH8 node %d reached twice", node));
+        node_seen[node] = 1;
+        if (depth > kMaxDepth)
+            return fail(format("BVH8 depth %u exceeds %u", depth, kMaxDepth));
+        const igxrt_bvh8_node& n = b.nodes8[node];
+        if (!n.valid)
+            return fail(format("BVH8 node %d has no slot", node));
+        const uint8_t* q[3][2] = {{n.lo_x, n.hi_x}, {n.lo_y, n.hi_y}, {n.lo_z, n.hi_z}};
+        for (int a = 0; a < 3; ++a)
+            if (n.exp[a] < -126 || !std::isfinite(n.origin[a]))
+                return fail(format("BVH8 node %d has a bad grid", node));
+        content.reset();
+        for (int c = 0; c < 8; ++c) {
+            if (!(n.valid >> c & 1))
+                continue;
+            if (b.src8[8 * (size_t)node + c] >= 2 * b.nodes2.size())
+                return fail(format("BVH8 node %d slot %d has no BVH2 source", node, c));
+            float lo[3], hi[3];
+            for (int a = 0; a < 3; ++a) {
+                const float s = ldexpf(1.f, n.exp[a]);
+                lo[a] = fmaf((float)q[a][0][c], s, n.origin[a]);
+                hi[a] = fmaf((float)q[a][1][c], s, n.origin[a]);
+            }
+            Aabb sub;
+            sub.reset();
+            if (n.child[c] < 0) {
+                if (!leaf(n.child[c], lo, hi))
+                    return false;
+                for (uint32_t i = (uint32_t)~n.child[c];; ++i) {
+                    bool finite;
+                    float unused = 0.f;
+                    sub.grow(object_bounds(d, b.prims[i].prim, finite, unused));
+                    if (b.prims[i].leaf_end)
+                        break;
+                }
+            } else {
+                if (!node8(d, n.child[c], depth + 1, sub))
+                    return false;
+                for (int a = 0; a < 3; ++a)
+                    if (!(sub.lo[a] >= lo[a] && sub.hi[a] <= hi[a]))
+                        return fail(format("BVH8 node %d slot %d does not hold its subtree", node, c));
+            }
+            content.grow(sub);
         }
         return true;
     }
@@ -1048,6 +1211,34 @@ igxrt_status validate_bvh(const igxrt_bvh& b, std::string& msg) {
             tri_seen[r.prim] = 1;
         }
     }
+    // BVH8 (optional: GPU builds and very deep trees have none)
+    if (b.info.bvh8_nodes != b.nodes8.size() || b.src8.size() != 8 * b.nodes8.size()) {
+        msg = "BVH8 arrays and info disagree";
+        return IGXRT_ERROR_INVALID_BVH;
+    }
+    if (!b.nodes8.empty()) {
+        Checker ck{b, msg, std::vector<uint8_t>(nt, 0), {}, std::vector<uint8_t>(b.nodes8.size(), 0)};
+        igxrt_scene_desc d{};
+        d.triangles = b.tris.data();
+        d.triangle_count = (uint32_t)b.tris.size();
+        d.spheres = b.spheres.data();
+        d.sphere_count = (uint32_t)(b.spheres.size() / 4);
+        d.cubes = b.cubes.data();
+        d.cube_count = (uint32_t)b.cubes.size();
+        Aabb all;
+        if (!ck.node8(d, 0, 1, all))
+            return IGXRT_ERROR_INVALID_BVH;
+        for (size_t i = 0; i < b.nodes8.size(); ++i)
+            if (!ck.node_seen[i]) {
+                msg = format("BVH8 node %zu unreachable", i);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+        for (size_t i = 0; i < nt; ++i)
+            if (!ck.rec_seen[i]) {
+                msg = format("primitive record %zu unreachable in BVH8", i);
+                return IGXRT_ERROR_INVALID_BVH;
+            }
+    }
     return IGXRT_OK;
 }
 
@@ -1067,9 +1258,10 @@ struct FileHeader {
     uint32_t abi;
     uint64_t tris, nodes2, nodes4, prims;
     uint64_t spheres, cubes, planes;
+    uint64_t nodes8;  // followed by 8 BVH2 sources per BVH8 node
     igxrt_bvh_info info;
 };
-constexpr uint32_t kFileVersion = 2;
+constexpr uint32_t kFileVersion = 3;
 
 constexpr char kMagic[8] = {'I', 'G', 'X', 'R', 'T', 'B', 'V', 'H'};
 
@@ -1157,10 +1349,13 @@ igxrt_status igxrt_bvh_get_data(const igxrt_bvh* bvh, uint32_t layout, const voi
     if (!bvh || layout >= IGXRT_LAYOUT_COUNT)
         return IGXRT_ERROR_INVALID_ARGUMENT;
     if (nodes)
-        *nodes = layout == IGXRT_LAYOUT_BVH2 ? (const void*)bvh->nodes2.data()
-                                             : (const void*)bvh->nodes4.data();
+        *nodes = layout == IGXRT_LAYOUT_BVH2   ? (const void*)bvh->nodes2.data()
+                 : layout == IGXRT_LAYOUT_BVH4 ? (const void*)bvh->nodes4.data()
+                                               : (const void*)bvh->nodes8.data();
     if (node_count)
-        *node_count = layout == IGXRT_LAYOUT_BVH2 ? bvh->nodes2.size() : bvh->nodes4.size();
+        *node_count = layout == IGXRT_LAYOUT_BVH2   ? bvh->nodes2.size()
+                      : layout == IGXRT_LAYOUT_BVH4 ? bvh->nodes4.size()
+                                                    : bvh->nodes8.size();
     if (prims)
         *prims = bvh->prims.data();
     if (prim_count)
@@ -1196,6 +1391,7 @@ igxrt_status igxrt_bvh_save(const igxrt_bvh* bvh, const char* path) {
     h.spheres = bvh->spheres.size() / 4;
     h.cubes = bvh->cubes.size();
     h.planes = bvh->planes.size() / 4;
+    h.nodes8 = bvh->nodes8.size();
     h.info = bvh->info;
     bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
     ok = ok && fwrite(bvh->tris.data(), sizeof(igxrt_triangle), h.tris, f) == h.tris;
@@ -1205,6 +1401,8 @@ igxrt_status igxrt_bvh_save(const igxrt_bvh* bvh, const char* path) {
     ok = ok && fwrite(bvh->spheres.data(), 16, h.spheres, f) == h.spheres;
     ok = ok && fwrite(bvh->cubes.data(), sizeof(igxrt_cube), h.cubes, f) == h.cubes;
     ok = ok && fwrite(bvh->planes.data(), 16, h.planes, f) == h.planes;
+    ok = ok && fwrite(bvh->nodes8.data(), sizeof(igxrt_bvh8_node), h.nodes8, f) == h.nodes8;
+    ok = ok && fwrite(bvh->src8.data(), 32, h.nodes8, f) == h.nodes8;
     ok = (fclose(f) == 0) && ok;
     return ok ? IGXRT_OK : IGXRT_ERROR_IO;
 }
@@ -1225,7 +1423,7 @@ igxrt_status igxrt_bvh_load(const char* path, igxrt_bvh** out) {
         const uint64_t objects = h.tris + h.spheres + h.cubes;
         if (h.tris >= 0x7fffffffu || h.spheres >= 0x7fffffffu || h.cubes >= 0x7fffffffu ||
             h.planes >= 0x7fffffffu || objects + h.planes >= 0x7fffffffu || h.prims != objects ||
-            h.nodes2 > 2 * objects + 1 || h.nodes4 > 2 * objects + 1)
+            h.nodes2 > 2 * objects + 1 || h.nodes4 > 2 * objects + 1 || h.nodes8 > 2 * objects + 1)
             break;
         b = new (std::nothrow) igxrt_bvh();
         if (!b) {
@@ -1239,13 +1437,17 @@ igxrt_status igxrt_bvh_load(const char* path, igxrt_bvh** out) {
         b->spheres.resize(4 * h.spheres);
         b->cubes.resize(h.cubes);
         b->planes.resize(4 * h.planes);
+        b->nodes8.resize(h.nodes8);
+        b->src8.resize(8 * h.nodes8);
         if (fread(b->tris.data(), sizeof(igxrt_triangle), h.tris, f) != h.tris ||
             fread(b->nodes2.data(), sizeof(igxrt_bvh2_node), h.nodes2, f) != h.nodes2 ||
             fread(b->nodes4.data(), sizeof(igxrt_bvh4_node), h.nodes4, f) != h.nodes4 ||
             fread(b->prims.data(), sizeof(igxrt_prim_record), h.prims, f) != h.prims ||
             fread(b->spheres.data(), 16, h.spheres, f) != h.spheres ||
             fread(b->cubes.data(), sizeof(igxrt_cube), h.cubes, f) != h.cubes ||
-            fread(b->planes.data(), 16, h.planes, f) != h.planes)
+            fread(b->planes.data(), 16, h.planes, f) != h.planes ||
+            fread(b->nodes8.data(), sizeof(igxrt_bvh8_node), h.nodes8, f) != h.nodes8 ||
+            fread(b->src8.data(), 32, h.nodes8, f) != h.nodes8)
             break;
         b->info = h.info;
         std::string m;

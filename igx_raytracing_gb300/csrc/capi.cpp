@@ -75,10 +75,11 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
 
 // One device allocation per scene, 256-byte aligned sub-buffers in this
 // order: BVH2 nodes, BVH4 nodes, records, triangles, planes, parent links of
-// both layouts, refit words.  Fills every pointer and count of the scene from
-// `info` and the node counts; the contents are the caller's to write.
+// BVH2 and BVH4, refit words, BVH8 nodes, BVH8 slot sources.  Fills every
+// pointer and count of the scene from `info` and the node counts; the
+// contents are the caller's to write.
 igxrt_status allocate_scene(igxrt_context* ctx, const igxrt_bvh_info& info, uint32_t n2, uint32_t n4,
-                            igxrt_scene*& out) {
+                            uint32_t n8, igxrt_scene*& out) {
     out = nullptr;
     igxrt_scene* s = new (std::nothrow) igxrt_scene();
     if (!s)
@@ -94,12 +95,18 @@ igxrt_status allocate_scene(igxrt_context* ctx, const igxrt_bvh_info& info, uint
     const size_t nn = (size_t)n2 + n4;
     const size_t bpar = round_up(nn * sizeof(uint32_t), 256);
     const size_t bw = round_up((kRefitStateWords + nn) * sizeof(uint32_t), 256);
-    cudaError_t e = cudaMalloc(&s->d_mem, b2 + b4 + bp + bt + bl + bpar + bw);
+    const size_t b8 = round_up((size_t)n8 * sizeof(igxrt_bvh8_node), 256);
+    const size_t bs8 = round_up((size_t)n8 * 8 * sizeof(uint32_t), 256);
+    const size_t o8 = b2 + b4 + bp + bt + bl + bpar + bw;
+    cudaError_t e = cudaMalloc(&s->d_mem, o8 + b8 + bs8);
     if (e != cudaSuccess) {
         delete s;
         return cuda_fail(ctx, e, "scene allocation");
     }
     char* base = (char*)s->d_mem;
+    s->nodes[IGXRT_LAYOUT_BVH8] = base + o8;
+    s->node_count[IGXRT_LAYOUT_BVH8] = n8;
+    s->src8 = (const uint32_t*)(base + o8 + b8);
     s->nodes[IGXRT_LAYOUT_BVH2] = base;
     s->nodes[IGXRT_LAYOUT_BVH4] = base + b2;
     s->prims = (const igxrt_prim_record*)(base + b2 + b4);
@@ -215,6 +222,9 @@ igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const ig
     st = resolve_params(ctx, params, p);
     if (st != IGXRT_OK)
         return st;
+    if (!scene->has_layout(p.layout))
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED,
+                    format("the scene has no layout %u (GPU-built trees have BVH2 and BVH4)", p.layout));
     DeviceGuard guard(ctx->device);
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
@@ -386,7 +396,7 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
     }
     igxrt_scene* s = nullptr;
     igxrt_status st = allocate_scene(ctx, bvh->info, (uint32_t)bvh->nodes2.size(),
-                                     (uint32_t)bvh->nodes4.size(), s);
+                                     (uint32_t)bvh->nodes4.size(), (uint32_t)bvh->nodes8.size(), s);
     if (st != IGXRT_OK)
         return st;
     cudaError_t e = cudaSuccess;
@@ -394,6 +404,8 @@ igxrt_status igxrt_scene_create_from_bvh(igxrt_context* ctx, const igxrt_bvh* bv
         if (e == cudaSuccess && bytes)
             e = cudaMemcpy(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice);
     };
+    up(s->nodes[IGXRT_LAYOUT_BVH8], bvh->nodes8.data(), bvh->nodes8.size() * sizeof(igxrt_bvh8_node));
+    up(s->src8, bvh->src8.data(), bvh->src8.size() * sizeof(uint32_t));
     up(s->parents[IGXRT_LAYOUT_BVH2], par2.data(), par2.size() * sizeof(uint32_t));
     up(s->parents[IGXRT_LAYOUT_BVH4], par4.data(), par4.size() * sizeof(uint32_t));
     up(s->planes, bvh->planes.data(), bvh->planes.size() * sizeof(float));
@@ -486,6 +498,8 @@ igxrt_status igxrt_scene_download(igxrt_context* ctx, const igxrt_scene* scene, 
         b->info = info;
         b->nodes2.resize(scene->node_count[IGXRT_LAYOUT_BVH2]);
         b->nodes4.resize(scene->node_count[IGXRT_LAYOUT_BVH4]);
+        b->nodes8.resize(scene->node_count[IGXRT_LAYOUT_BVH8]);
+        b->src8.resize(8 * (size_t)scene->node_count[IGXRT_LAYOUT_BVH8]);
         b->prims.resize(records);
         b->tris.resize(info.triangle_count);
         b->planes.resize(4 * (size_t)info.plane_count);
@@ -502,6 +516,8 @@ igxrt_status igxrt_scene_download(igxrt_context* ctx, const igxrt_scene* scene, 
     };
     down(b->nodes2.data(), scene->nodes[IGXRT_LAYOUT_BVH2], b->nodes2.size() * sizeof(igxrt_bvh2_node));
     down(b->nodes4.data(), scene->nodes[IGXRT_LAYOUT_BVH4], b->nodes4.size() * sizeof(igxrt_bvh4_node));
+    down(b->nodes8.data(), scene->nodes[IGXRT_LAYOUT_BVH8], b->nodes8.size() * sizeof(igxrt_bvh8_node));
+    down(b->src8.data(), scene->src8, b->src8.size() * sizeof(uint32_t));
     down(b->prims.data(), scene->prims, records * sizeof(igxrt_prim_record));
     down(b->tris.data(), scene->tris, b->tris.size() * sizeof(igxrt_triangle));
     down(b->planes.data(), scene->planes, b->planes.size() * sizeof(float));

@@ -37,8 +37,8 @@ struct igxrt_scene {
     int device = 0;
     igxrt_bvh_info info{};
     void* d_mem = nullptr;
-    const void* nodes[IGXRT_LAYOUT_COUNT] = {nullptr, nullptr};
-    uint32_t node_count[IGXRT_LAYOUT_COUNT] = {0, 0};
+    const void* nodes[IGXRT_LAYOUT_COUNT] = {nullptr, nullptr, nullptr};
+    uint32_t node_count[IGXRT_LAYOUT_COUNT] = {0, 0, 0};
     const igxrt_prim_record* prims = nullptr;
     const igxrt_triangle* tris = nullptr;
     // mixed scenes: spheres and cubes are in the tree, planes are not
@@ -49,8 +49,17 @@ struct igxrt_scene {
     // refit: the parent of every node per layout (kNoParent at the root), and
     // kRefitStateWords state words followed by one arrival counter per node
     // of BVH2, then of BVH4 (zeroed before each refit)
-    const uint32_t* parents[IGXRT_LAYOUT_COUNT] = {nullptr, nullptr};
+    const uint32_t* parents[IGXRT_LAYOUT_COUNT] = {nullptr, nullptr, nullptr};
     uint32_t* refit_words = nullptr;
+    // BVH8 slots' sources in the BVH2 layout (8 per BVH8 node), for the refit
+    const uint32_t* src8 = nullptr;
+
+    // A layout can be traced when the tree has it; an empty scene has none
+    // and traces as all misses in every layout.
+    bool has_layout(uint32_t layout) const {
+        return layout < IGXRT_LAYOUT_COUNT &&
+               (node_count[layout] > 0 || info.triangle_count + info.sphere_count + info.cube_count == 0);
+    }
 };
 
 namespace igxrt {
@@ -62,9 +71,9 @@ constexpr uint32_t kRefitStateWords = 8;
 inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // One device allocation for a scene of `info`'s primitive counts and n2 / n4
-// nodes; every pointer of the scene is set, the contents are unwritten.
+// / n8 nodes; every pointer of the scene is set, the contents are unwritten.
 igxrt_status allocate_scene(igxrt_context* ctx, const igxrt_bvh_info& info, uint32_t n2, uint32_t n4,
-                            igxrt_scene*& out);
+                            uint32_t n8, igxrt_scene*& out);
 
 // Parent links of both layouts, computed on the host at scene creation and
 // stored after the scene's other buffers (see refit.cu).

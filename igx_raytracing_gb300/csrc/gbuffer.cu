@@ -157,6 +157,8 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     st = resolve_params(ctx, ctx->params, p);
     if (st != IGXRT_OK)
         return st;
+    if (!scene->has_layout(p.layout))
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, format("the scene has no layout %u", p.layout));
     DeviceGuard guard(ctx->device);
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
@@ -193,7 +195,9 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     a.uv_normal = d_uv;
     a.status = status_word(ctx);
     a.sh_depth = p.stack_depth;
-    auto fn = p.layout == IGXRT_LAYOUT_BVH4 ? gbuffer_kernel<IGXRT_LAYOUT_BVH4> : gbuffer_kernel<IGXRT_LAYOUT_BVH2>;
+    auto fn = p.layout == IGXRT_LAYOUT_BVH8   ? gbuffer_kernel<IGXRT_LAYOUT_BVH8>
+              : p.layout == IGXRT_LAYOUT_BVH4 ? gbuffer_kernel<IGXRT_LAYOUT_BVH4>
+                                              : gbuffer_kernel<IGXRT_LAYOUT_BVH2>;
     const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
     cudaError_t e = allow_smem((const void*)fn, smem);

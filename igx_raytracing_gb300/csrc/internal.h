@@ -1,6 +1,8 @@
 // internal.h — shared host-side definitions of the ray-query engine.
 #pragma once
 
+#include <math.h>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -26,11 +28,106 @@ struct igxrt_bvh {
     std::vector<float> planes;       // 4 per plane: normal, offset (outside the tree)
     std::vector<igxrt_bvh2_node> nodes2;
     std::vector<igxrt_bvh4_node> nodes4;
+    std::vector<igxrt_bvh8_node> nodes8;
+    // per BVH8 node and slot: where the slot's exact (padded) box lives in the
+    // BVH2 layout, 2 * node + slot, kNoSource for an empty slot (the refit
+    // re-quantizes BVH8 nodes from these boxes)
+    std::vector<uint32_t> src8;
     std::vector<igxrt_prim_record> prims;
     igxrt_bvh_info info{};
 };
 
 namespace igxrt {
+
+constexpr uint32_t kNoSource = 0xffffffffu;
+
+#ifdef __CUDACC__
+#define IGXRT_HD __host__ __device__
+#else
+#define IGXRT_HD
+#endif
+
+// BVH8 quantization, compiled for the host builder and refit and for the GPU
+// refit from this one definition so both produce the same bytes.  A node's
+// grid on one axis has origin = the node's lo and step 2^exp, exp the
+// smallest integer in [-126, 127] whose 255 steps, decoded in binary32,
+// reach the node's hi.  A slot gets the largest lo byte and the smallest hi
+// byte whose decodings fmaf(q, 2^exp, origin) still enclose its box.  The
+// decoding is monotone in q, byte 0 decodes to origin <= every slot's lo and
+// byte 255 to at least hi, so both searches end inside [0, 255].
+IGXRT_HD inline int bvh8_exponent(float lo, float hi) {
+    int k = 0;
+    const double ext = (double)hi - (double)lo;
+    if (ext > 0.0)
+        frexp(ext, &k);
+    int e = k - 8 < -126 ? -126 : (k - 8 > 127 ? 127 : k - 8);
+    while (e < 127 && fmaf(255.f, ldexpf(1.f, e), lo) < hi)
+        ++e;
+    while (e > -126 && fmaf(255.f, ldexpf(1.f, e - 1), lo) >= hi)
+        --e;
+    return e;
+}
+
+IGXRT_HD inline void bvh8_quantize(float origin, int exp, float lo, float hi, uint8_t& qlo, uint8_t& qhi) {
+    const float s = ldexpf(1.f, exp);
+    const double step = ldexp(1.0, exp);
+    double ea = floor(((double)lo - (double)origin) / step);
+    double eb = ceil(((double)hi - (double)origin) / step);
+    int a = (int)(ea < 0.0 ? 0.0 : (ea > 255.0 ? 255.0 : ea));
+    int b = (int)(eb < 0.0 ? 0.0 : (eb > 255.0 ? 255.0 : eb));
+    while (a > 0 && fmaf((float)a, s, origin) > lo)
+        --a;
+    while (a < 255 && fmaf((float)(a + 1), s, origin) <= lo)
+        ++a;
+    while (b < 255 && fmaf((float)b, s, origin) < hi)
+        ++b;
+    while (b > 0 && fmaf((float)(b - 1), s, origin) >= hi)
+        --b;
+    qlo = (uint8_t)a;
+    qhi = (uint8_t)b;
+}
+
+// Origin, exponents and bytes of a BVH8 node from the exact boxes of its
+// slots, which live in the BVH2 layout at src[c] = 2 * node + slot
+// (kNoSource for an empty slot).  `valid` and `child` are left as they are.
+IGXRT_HD inline void bvh8_quantize_node(const igxrt_bvh2_node* nodes2, const uint32_t* src,
+                                        igxrt_bvh8_node& n) {
+    float lo[8][3], hi[8][3];
+    float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+        if (src[c] == kNoSource)
+            continue;
+        const igxrt_bvh2_node& m = nodes2[src[c] >> 1];
+        const int s = (int)(src[c] & 1u);
+        const float* x = s ? m.c1_x : m.c0_x;
+        const float* y = s ? m.c1_y : m.c0_y;
+        const float* z = s ? m.c1_z : m.c0_z;
+        lo[c][0] = x[0];
+        hi[c][0] = x[1];
+        lo[c][1] = y[0];
+        hi[c][1] = y[1];
+        lo[c][2] = z[0];
+        hi[c][2] = z[1];
+        for (int a = 0; a < 3; ++a) {
+            nlo[a] = lo[c][a] < nlo[a] ? lo[c][a] : nlo[a];
+            nhi[a] = nhi[a] < hi[c][a] ? hi[c][a] : nhi[a];
+        }
+    }
+    int e[3];
+    for (int a = 0; a < 3; ++a) {
+        e[a] = bvh8_exponent(nlo[a], nhi[a]);
+        n.origin[a] = nlo[a];
+        n.exp[a] = (int8_t)e[a];
+    }
+    uint8_t* q[3][2] = {{n.lo_x, n.hi_x}, {n.lo_y, n.hi_y}, {n.lo_z, n.hi_z}};
+    for (int c = 0; c < 8; ++c)
+        for (int a = 0; a < 3; ++a) {
+            if (src[c] == kNoSource)
+                q[a][0][c] = q[a][1][c] = 0;
+            else
+                bvh8_quantize(nlo[a], e[a], lo[c][a], hi[c][a], q[a][0][c], q[a][1][c]);
+        }
+}
 
 // Thread-safe formatted message helper.
 std::string format(const char* fmt, ...);

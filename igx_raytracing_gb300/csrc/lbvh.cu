@@ -636,7 +636,7 @@ igxrt_status igxrt_scene_create_gpu(igxrt_context* ctx, const igxrt_scene_desc* 
                                kStackCapacity));
 
     igxrt_scene* scene = nullptr;
-    if ((st = allocate_scene(ctx, info, n2, n4, scene)) != IGXRT_OK)
+    if ((st = allocate_scene(ctx, info, n2, n4, 0, scene)) != IGXRT_OK)
         return st;
     auto copy = [&](const void* dst, const void* src, size_t bytes) {
         if (e == cudaSuccess && bytes)

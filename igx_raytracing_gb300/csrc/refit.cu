@@ -117,6 +117,9 @@ struct RefitArgs {
     const uint32_t* parents4;
     uint32_t n2, n4;
     uint32_t* state;  // kRefitStateWords, then arrival counters (n2, then n4)
+    igxrt_bvh8_node* nodes8;
+    const uint32_t* src8;
+    uint32_t n8;
 };
 
 static_assert(kRefitStateWords == 8, "refit state words");
@@ -224,6 +227,19 @@ __global__ void refit_nodes_kernel(RefitArgs a) {
         refit_climb<IGXRT_LAYOUT_BVH4>(a, i - a.n2, pad);
 }
 
+// Pass 4: every BVH8 node re-quantized from the refit BVH2 boxes of its
+// slots (the host refit calls the same bvh8_quantize_node).
+__global__ void refit_bvh8_kernel(RefitArgs a) {
+    if (a.state[kWordBad])
+        return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n8)
+        return;
+    igxrt_bvh8_node n = a.nodes8[i];
+    bvh8_quantize_node(static_cast<const igxrt_bvh2_node*>(a.nodes2), a.src8 + 8 * (size_t)i, n);
+    a.nodes8[i] = n;
+}
+
 }  // namespace
 
 extern "C" {
@@ -264,6 +280,9 @@ igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igx
     a.n2 = scene->node_count[IGXRT_LAYOUT_BVH2];
     a.n4 = scene->node_count[IGXRT_LAYOUT_BVH4];
     a.state = scene->refit_words;
+    a.nodes8 = static_cast<igxrt_bvh8_node*>(const_cast<void*>(scene->nodes[IGXRT_LAYOUT_BVH8]));
+    a.src8 = scene->src8;
+    a.n8 = scene->node_count[IGXRT_LAYOUT_BVH8];
 
     const uint32_t n = a.obj.count();
     const size_t words = kRefitStateWords + (size_t)a.n2 + a.n4;
@@ -278,6 +297,8 @@ igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igx
     const uint32_t nodes = a.n2 + a.n4;
     if (nodes)
         refit_nodes_kernel<<<(nodes + 127) / 128, 128, 0, s>>>(a);
+    if (a.n8)
+        refit_bvh8_kernel<<<(a.n8 + 127) / 128, 128, 0, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "refit launch");
@@ -323,7 +344,9 @@ igxrt_status igxrt_scene_read_bvh(igxrt_context* ctx, const igxrt_scene* scene, 
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
     cudaError_t e = cudaDeviceSynchronize();
-    const size_t node_bytes = layout == IGXRT_LAYOUT_BVH2 ? sizeof(igxrt_bvh2_node) : sizeof(igxrt_bvh4_node);
+    const size_t node_bytes = layout == IGXRT_LAYOUT_BVH2   ? sizeof(igxrt_bvh2_node)
+                              : layout == IGXRT_LAYOUT_BVH4 ? sizeof(igxrt_bvh4_node)
+                                                            : sizeof(igxrt_bvh8_node);
     if (e == cudaSuccess && nodes && node_count)
         e = cudaMemcpy(nodes, scene->nodes[layout], node_bytes * node_count, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && prims && prim_count)

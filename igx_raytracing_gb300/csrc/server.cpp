@@ -336,6 +336,10 @@ igxrt_status igxrt_server_add_scene(igxrt_server* s, const igxrt_scene* scene, u
         return IGXRT_ERROR_INVALID_ARGUMENT;
     if (scene->device != s->ctx->device)
         return IGXRT_ERROR_INVALID_ARGUMENT;
+    // the batched kernel the server launches traces triangle-only trees in
+    // the server's layout
+    if (scene->mixed || !scene->has_layout(s->params.layout))
+        return IGXRT_ERROR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(s->mu);
     *scene_id = (uint32_t)s->scenes.size();
     s->scenes.push_back(scene);

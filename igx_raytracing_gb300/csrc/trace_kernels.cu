@@ -163,11 +163,18 @@ using KernelFn = void (*)(KernelArgs);
 // Instrumented variants exist for triangle-only scenes; mixed scenes have
 // no host traversal to compare counts with.
 static KernelFn select_kernel(uint32_t layout, bool any, bool count, bool mixed) {
-    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4;
+    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
     if (mixed) {
+        if (layout == B8)
+            return any ? trace_kernel<B8, true, false, true> : trace_kernel<B8, false, false, true>;
         if (layout == B4)
             return any ? trace_kernel<B4, true, false, true> : trace_kernel<B4, false, false, true>;
         return any ? trace_kernel<B2, true, false, true> : trace_kernel<B2, false, false, true>;
+    }
+    if (layout == B8) {
+        if (count)
+            return any ? trace_kernel<B8, true, true, false> : trace_kernel<B8, false, true, false>;
+        return any ? trace_kernel<B8, true, false, false> : trace_kernel<B8, false, false, false>;
     }
     if (layout == B4) {
         if (count)

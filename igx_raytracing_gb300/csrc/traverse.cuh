@@ -233,6 +233,65 @@ __device__ __forceinline__ bool box_test(const RayState& r, float lox, float hix
                  : box_hit(r, lox, hix, loy, hiy, loz, hiz, tcull, tn);
 }
 
+// BVH8 slot order: the entry distance as an order-preserving word whose low
+// 3 bits are replaced by the slot, so keys are distinct and sort by
+// (distance, slot).  A pushed entry keeps the distance of the key with those
+// bits cleared, never larger than the box's own (the host traversal does the
+// same).
+__device__ __forceinline__ uint32_t slot_key(float t, uint32_t slot) {
+    const uint32_t u = __float_as_uint(t);
+    return (((u & 0x80000000u) ? ~u : (u | 0x80000000u)) & ~7u) | slot;
+}
+
+__device__ __forceinline__ float key_distance(uint32_t k) {
+    k &= ~7u;
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__device__ __forceinline__ void sort2(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+// Byte `i` of a little-endian word pair as an exact float: the byte placed
+// in the mantissa of 2^23 (one byte permute), minus 2^23.
+__device__ __forceinline__ float byte_float(float w0, float w1, int i) {
+    const uint32_t w = __float_as_uint(i < 4 ? w0 : w1);
+    return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)(i & 3))),
+                     8388608.0f);
+}
+
+// A ray-space step that is a finite normal float (its product with a byte
+// and the sum with the offset then round like the world-space test).
+__device__ __forceinline__ bool ray_space_ok(float m) {
+    const float a = fabsf(m);
+    return a >= 1.17549435e-38f && a <= 3.4028235e38f;
+}
+
+// box_hit / box_hit_mixed with each axis' entry and exit distances given
+// (near and far planes already told apart by the direction's sign).
+template <bool MIXED>
+__device__ __forceinline__ bool slab_test(const RayState& r, float tnx, float tfx, float tny, float tfy,
+                                          float tnz, float tfz, float tcull, float& tn) {
+    if (MIXED) {
+        const float tnear = fmaxf(fmaxf(tnx, tny), tnz);
+        const float tslab = fminf(fminf(tfx, tfy), tfz);
+        tn = tnear;
+        return tslab >= r.tmin_box && tnear <= fminf(tslab, tcull);
+    }
+    const float tnear = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin_box));
+    const float tfar = fminf(fminf(tfx, tfy), fminf(tfz, tcull));
+    tn = tnear;
+    return tnear <= tfar;
+}
+
+__device__ __forceinline__ int32_t pick8(const float4& c0, const float4& c1, uint32_t slot) {
+    const float4& c = (slot & 4u) ? c1 : c0;
+    const float v = (slot & 2u) ? ((slot & 1u) ? c.w : c.z) : ((slot & 1u) ? c.y : c.x);
+    return __float_as_int(v);
+}
+
 // One interior-node visit in the kernels' order: test the children, descend
 // into the nearer hit child and push the other.  Returns the next reference
 // (a node, a leaf, or kRefDone), or sets `overflow`.
@@ -242,7 +301,90 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
                                               TraversalStack& st, bool& overflow, uint32_t& nf) {
     if (COUNT)
         ++nf;
-    if (LAYOUT == IGXRT_LAYOUT_BVH4) {
+    if (LAYOUT == IGXRT_LAYOUT_BVH8) {
+        // 96-byte node: {origin, exp bytes + valid}{lo_x, hi_x} {lo_y, hi_y, lo_z, hi_z} {child[8]}
+        const float4* n = nodes + 6 * (size_t)node;
+        float4 hdr, qx, qy, qz, c0, c1;
+        ldg256(n, hdr, qx);
+        ldg256(n + 2, qy, qz);
+        ldg256(n + 4, c0, c1);
+        const uint32_t meta = __float_as_uint(hdr.w);
+        // 2^exp as a float (exp in [-126, 127], checked by the validator)
+        const float sx = __int_as_float(((int)(int8_t)(meta & 0xffu) + 127) << 23);
+        const float sy = __int_as_float(((int)(int8_t)((meta >> 8) & 0xffu) + 127) << 23);
+        const float sz = __int_as_float(((int)(int8_t)((meta >> 16) & 0xffu) + 127) << 23);
+        const uint32_t valid = meta >> 24;
+        uint32_t k[8];
+        uint32_t m = 0;
+        // Ray space: a plane q steps from the origin lies at
+        // t = fmaf(q, 2^exp * (1/d), fmaf(origin, 1/d, -o/d)), one product
+        // scaled by a power of two (exact while it stays a normal float) and
+        // two roundings, like box_hit's fmaf(plane, 1/d, -o/d).  With a
+        // positive step the lo byte is the near plane, else the hi byte.
+        const float mx = __fmul_rn(sx, r.ix), my = __fmul_rn(sy, r.iy), mz = __fmul_rn(sz, r.iz);
+        const float bx = __fmaf_rn(hdr.x, r.ix, -r.oix), by = __fmaf_rn(hdr.y, r.iy, -r.oiy),
+                    bz = __fmaf_rn(hdr.z, r.iz, -r.oiz);
+        const bool fast = ray_space_ok(mx) && ray_space_ok(my) && ray_space_ok(mz) &&
+                          fabsf(bx) <= 3.4028235e38f && fabsf(by) <= 3.4028235e38f &&
+                          fabsf(bz) <= 3.4028235e38f;
+        if (fast) {
+            const bool px = mx > 0.f, py = my > 0.f, pz = mz > 0.f;
+            const float nx0 = px ? qx.x : qx.z, nx1 = px ? qx.y : qx.w, fx0 = px ? qx.z : qx.x,
+                        fx1 = px ? qx.w : qx.y;
+            const float ny0 = py ? qy.x : qy.z, ny1 = py ? qy.y : qy.w, fy0 = py ? qy.z : qy.x,
+                        fy1 = py ? qy.w : qy.y;
+            const float nz0 = pz ? qz.x : qz.z, nz1 = pz ? qz.y : qz.w, fz0 = pz ? qz.z : qz.x,
+                        fz1 = pz ? qz.w : qz.y;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const float tnx = __fmaf_rn(byte_float(nx0, nx1, c), mx, bx);
+                const float tfx = __fmaf_rn(byte_float(fx0, fx1, c), mx, bx);
+                const float tny = __fmaf_rn(byte_float(ny0, ny1, c), my, by);
+                const float tfy = __fmaf_rn(byte_float(fy0, fy1, c), my, by);
+                const float tnz = __fmaf_rn(byte_float(nz0, nz1, c), mz, bz);
+                const float tfz = __fmaf_rn(byte_float(fz0, fz1, c), mz, bz);
+                float tn;
+                const bool h = slab_test<MIXED>(r, tnx, tfx, tny, tfy, tnz, tfz, best.tcull, tn) &&
+                               ((valid >> c) & 1u);
+                k[c] = h ? slot_key(tn, (uint32_t)c) : 0xffffffffu;
+                m += h ? 1u : 0u;
+            }
+        } else {
+            // a step out of the normal range: decode the planes in world space
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const float lox = __fmaf_rn(byte_float(qx.x, qx.y, c), sx, hdr.x);
+                const float hix = __fmaf_rn(byte_float(qx.z, qx.w, c), sx, hdr.x);
+                const float loy = __fmaf_rn(byte_float(qy.x, qy.y, c), sy, hdr.y);
+                const float hiy = __fmaf_rn(byte_float(qy.z, qy.w, c), sy, hdr.y);
+                const float loz = __fmaf_rn(byte_float(qz.x, qz.y, c), sz, hdr.z);
+                const float hiz = __fmaf_rn(byte_float(qz.z, qz.w, c), sz, hdr.z);
+                float tn;
+                const bool h = box_test<MIXED>(r, lox, hix, loy, hiy, loz, hiz, best.tcull, tn) &&
+                               ((valid >> c) & 1u);
+                k[c] = h ? slot_key(tn, (uint32_t)c) : 0xffffffffu;
+                m += h ? 1u : 0u;
+            }
+        }
+        if (m == 0)
+            return st.pop_live(best.tcull);
+        // ascending keys: the optimal 19-comparator network for 8 inputs
+        sort2(k[0], k[2]); sort2(k[1], k[3]); sort2(k[4], k[6]); sort2(k[5], k[7]);
+        sort2(k[0], k[4]); sort2(k[1], k[5]); sort2(k[2], k[6]); sort2(k[3], k[7]);
+        sort2(k[0], k[1]); sort2(k[2], k[3]); sort2(k[4], k[5]); sort2(k[6], k[7]);
+        sort2(k[2], k[4]); sort2(k[3], k[5]);
+        sort2(k[1], k[4]); sort2(k[3], k[6]);
+        sort2(k[1], k[2]); sort2(k[3], k[4]); sort2(k[5], k[6]);
+        if (st.sp + m - 1 > kStackCapacityDevice) {
+            overflow = true;
+            return kRefDone;
+        }
+#pragma unroll
+        for (int j = 7; j >= 1; --j)
+            if ((uint32_t)j < m)
+                st.push(pick8(c0, c1, k[j] & 7u), key_distance(k[j]));
+        return pick8(c0, c1, k[0] & 7u);
+    } else if (LAYOUT == IGXRT_LAYOUT_BVH4) {
         const float4* n = nodes + 8 * (size_t)node;
         float4 lx, hx, ly, hy, lz, hz, c, unused;
         ldg256(n, lx, hx);

@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define IGXRT_ABI_VERSION 1u
+#define IGXRT_ABI_VERSION 2u
 
 /* res/shaders/primitive.glsl:6-7: the miss distance and the "no object" id. */
 #define IGXRT_NO_HIT 3.4028235e38f
@@ -112,7 +112,8 @@ typedef struct igxrt_hit {
 /* Node layouts the builder can emit. */
 #define IGXRT_LAYOUT_BVH2 0u /* binary, 64-byte nodes holding both child boxes */
 #define IGXRT_LAYOUT_BVH4 1u /* 4-wide, 128-byte nodes holding four child boxes */
-#define IGXRT_LAYOUT_COUNT 2u
+#define IGXRT_LAYOUT_BVH8 2u /* 8-wide, 96-byte nodes with 8-bit quantized child boxes */
+#define IGXRT_LAYOUT_COUNT 3u
 
 /*
  * BVH2 node, 64 bytes, 64-byte aligned; read as four 128-bit loads.
@@ -142,6 +143,23 @@ typedef struct igxrt_bvh4_node {
     int32_t child[4];
     uint32_t pad[4];
 } igxrt_bvh4_node;
+
+/*
+ * BVH8 node, 96 bytes, 32-byte aligned; read as three 256-bit loads.  Child
+ * c's box on axis a is [origin[a] + lo_a[c] * 2^exp[a], origin[a] + hi_a[c] *
+ * 2^exp[a]], each bound decoded as fmaf(q, 2^exp[a], origin[a]) in binary32;
+ * the builder rounds the bytes outward so the decoded box contains the child's
+ * padded box.  Bit c of `valid` marks a used slot; child[c] as in BVH2.
+ */
+typedef struct igxrt_bvh8_node {
+    float origin[3];
+    int8_t exp[3];
+    uint8_t valid;
+    uint8_t lo_x[8], hi_x[8];
+    uint8_t lo_y[8], hi_y[8];
+    uint8_t lo_z[8], hi_z[8];
+    int32_t child[8];
+} igxrt_bvh8_node;
 
 /*
  * Primitive record, 48 bytes, in leaf order.  e1 = p1 - p0 and e2 = p2 - p0
@@ -203,6 +221,7 @@ typedef struct igxrt_bvh_info {
     float bounds[6]; /* min xyz, max xyz of the triangles */
     float pad_abs;   /* absolute outward padding added to every node box */
     uint32_t max_stack[IGXRT_LAYOUT_COUNT]; /* deepest traversal stack per layout */
+    uint32_t bvh8_nodes; /* 0: the tree has no BVH8 layout (GPU builds) */
     uint64_t device_bytes;
     uint32_t sphere_count, cube_count, plane_count;
     uint32_t reserved;
@@ -488,7 +507,9 @@ typedef struct igxrt_server_stats {
  * context must not be used by other threads while the server runs. */
 igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options* opts,
                                  igxrt_server** out);
-/* Registers a resident scene; it must outlive the server. */
+/* Registers a resident scene; it must outlive the server.  Mixed scenes, and
+ * scenes without the server's node layout, are refused with
+ * IGXRT_ERROR_UNSUPPORTED. */
 igxrt_status igxrt_server_add_scene(igxrt_server* server, const igxrt_scene* scene,
                                     uint32_t* scene_id);
 /* Queues a request and returns at once.  A request whose buffers can never

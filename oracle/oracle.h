@@ -51,7 +51,7 @@ int orc_reintersect_f64(const igxrt_ray* ray, const igxrt_triangle* tri,
                         double* t, double* u, double* v);
 
 /*
- * BVH traversal on the CPU.  layout = IGXRT_LAYOUT_BVH2 or _BVH4; nodes and
+ * BVH traversal on the CPU.  layout = IGXRT_LAYOUT_BVH2, _BVH4 or _BVH8; nodes and
  * prims as returned by igxrt_bvh_get_data.  mode 0 = closest (out_hits),
  * mode 1 = any (out_occluded).  node_fetches / prim_fetches may be NULL.
  * Returns 0, or -1 on a malformed BVH (stack overflow / bad index).

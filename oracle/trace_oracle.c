@@ -915,6 +915,132 @@ static int bvh4_trace_one(const igxrt_bvh4_node* nodes, uint64_t nn,
     return 0;
 }
 
+/* BVH8 slot order key: the entry distance mapped to an order-preserving word
+ * with its low 3 bits replaced by the slot, so keys are distinct and sort by
+ * (distance, slot); a pushed entry keeps the distance of the key with those
+ * bits cleared, which is never larger than the box's own. */
+static inline uint32_t order_key(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+static inline int normal_step(float m) {
+    const float a = fabsf(m);
+    return a >= FLT_MIN && a <= FLT_MAX;
+}
+
+/* The slab test of box_hit on given per-axis plane distances. */
+static inline int slab_hit(const rayprep* r, float t0x, float t1x, float t0y, float t1y, float t0z,
+                           float t1z, float tcull, float* tnear) {
+    const float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)),
+                           fmaxf(fminf(t0z, t1z), r->tmin_box));
+    const float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)),
+                           fminf(fmaxf(t0z, t1z), tcull));
+    *tnear = tn;
+    return tn <= tf;
+}
+
+static inline float key_distance(uint32_t k) {
+    k &= ~7u;
+    const uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+/* BVH8 layout (include/igxrt.h igxrt_bvh8_node): slot boxes decoded as
+ * fmaf(q, 2^exp, origin), tested with box_hit, entered nearest first. */
+static int bvh8_trace_one(const igxrt_bvh8_node* nodes, uint64_t nn,
+                          const igxrt_prim_record* prims, uint64_t np, const rayprep* r,
+                          int anyhit, best_hit* b, uint32_t* occluded, uint32_t* nf,
+                          uint32_t* pf) {
+    stack_entry stack[ORC_STACK];
+    int sp = 0;
+    *occluded = 0;
+    if (nn == 0)
+        return 0;
+    int32_t next = 0;
+    for (;;) {
+        if (next >= 0) {
+            if ((uint64_t)next >= nn)
+                return -1;
+            const igxrt_bvh8_node* n = &nodes[next];
+            ++*nf;
+            const float sx = ldexpf(1.f, n->exp[0]), sy = ldexpf(1.f, n->exp[1]),
+                        sz = ldexpf(1.f, n->exp[2]);
+            /* ray space: plane q at fmaf(q, 2^exp / d, fmaf(origin, 1/d, -o/d))
+             * while every step is a finite normal float; else world space */
+            const float mx = sx * r->idir.x, my = sy * r->idir.y, mz = sz * r->idir.z;
+            const float bx = fmaf(n->origin[0], r->idir.x, -r->ood.x);
+            const float by = fmaf(n->origin[1], r->idir.y, -r->ood.y);
+            const float bz = fmaf(n->origin[2], r->idir.z, -r->ood.z);
+            const int fast = normal_step(mx) && normal_step(my) && normal_step(mz) &&
+                             fabsf(bx) <= FLT_MAX && fabsf(by) <= FLT_MAX && fabsf(bz) <= FLT_MAX;
+            uint32_t key[8];
+            int m = 0;
+            for (int c = 0; c < 8; ++c) {
+                if (!(n->valid >> c & 1))
+                    continue;
+                float t;
+                int hit;
+                if (fast)
+                    hit = slab_hit(r, fmaf((float)n->lo_x[c], mx, bx), fmaf((float)n->hi_x[c], mx, bx),
+                                   fmaf((float)n->lo_y[c], my, by), fmaf((float)n->hi_y[c], my, by),
+                                   fmaf((float)n->lo_z[c], mz, bz), fmaf((float)n->hi_z[c], mz, bz),
+                                   b->tcull, &t);
+                else
+                    hit = box_hit(r, fmaf((float)n->lo_x[c], sx, n->origin[0]),
+                                  fmaf((float)n->hi_x[c], sx, n->origin[0]),
+                                  fmaf((float)n->lo_y[c], sy, n->origin[1]),
+                                  fmaf((float)n->hi_y[c], sy, n->origin[1]),
+                                  fmaf((float)n->lo_z[c], sz, n->origin[2]),
+                                  fmaf((float)n->hi_z[c], sz, n->origin[2]), b->tcull, &t);
+                if (!hit)
+                    continue;
+                const uint32_t k = (order_key(t) & ~7u) | (uint32_t)c;
+                int j = m++;
+                while (j > 0 && k < key[j - 1]) {
+                    key[j] = key[j - 1];
+                    --j;
+                }
+                key[j] = k;
+            }
+            if (m == 0) {
+                if (!pop_live(stack, &sp, b->tcull, &next))
+                    break;
+            } else {
+                if (sp + m - 1 > ORC_STACK)
+                    return -1;
+                for (int j = m - 1; j >= 1; --j) {
+                    stack[sp].ref = n->child[key[j] & 7u];
+                    stack[sp].tnear = key_distance(key[j]);
+                    ++sp;
+                }
+                next = n->child[key[0] & 7u];
+            }
+        } else {
+            uint64_t i = (uint64_t)(uint32_t)~next;
+            for (;;) {
+                if (i >= np)
+                    return -1;
+                const igxrt_prim_record* rec = &prims[i];
+                ++*pf;
+                if (leaf_record(r, rec, b, anyhit) && anyhit) {
+                    *occluded = 1;
+                    return 0;
+                }
+                if (rec->leaf_end)
+                    break;
+                ++i;
+            }
+            if (!pop_live(stack, &sp, b->tcull, &next))
+                break;
+        }
+    }
+    return 0;
+}
+
 typedef struct {
     uint32_t layout;
     const void* nodes;
@@ -946,6 +1072,9 @@ static void bvh_chunk(void* p, uint32_t b0, uint32_t e0) {
         int rc;
         if (c->layout == IGXRT_LAYOUT_BVH4)
             rc = bvh4_trace_one((const igxrt_bvh4_node*)c->nodes, c->nn, c->prims, c->np, &r,
+                                c->mode == 1, &b, &occ, &nf, &pf);
+        else if (c->layout == IGXRT_LAYOUT_BVH8)
+            rc = bvh8_trace_one((const igxrt_bvh8_node*)c->nodes, c->nn, c->prims, c->np, &r,
                                 c->mode == 1, &b, &occ, &nf, &pf);
         else
             rc = bvh2_trace_one((const igxrt_bvh2_node*)c->nodes, c->nn, c->prims, c->np, &r,

@@ -1,7 +1,7 @@
 """Host BVH builder (engine) + CPU traversal (oracle), no GPU needed.
 
 The CPU traversal visits the engine's exported BVH in the kernels' order; it
-must equal the brute-force linear loop bit for bit, in both node layouts.
+must equal the brute-force linear loop bit for bit, in every node layout.
 """
 import math
 import os
@@ -11,11 +11,11 @@ import pytest
 
 from conftest import (GOLDEN_CASES, assert_hits_equal, closest_rays, load_golden, nan_free,
                       occlusion_rays)
-from igx_raytracing_gb300 import BVH, IgxrtError, LAYOUT_BVH2, LAYOUT_BVH4, scenes
+from igx_raytracing_gb300 import BVH, IgxrtError, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, scenes
 from igx_raytracing_gb300._capi import TRIANGLE_DTYPE
 from oracle import pyoracle
 
-LAYOUTS = [LAYOUT_BVH2, LAYOUT_BVH4]
+LAYOUTS = [LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -170,3 +170,50 @@ def test_fetch_counts_are_layout_specific_and_positive():
     _, nf4, pf4 = pyoracle.bvh_trace(LAYOUT_BVH4, n4, p4, rays, counts=True)
     assert (nf2 >= 1).all() and (nf4 >= 1).all()
     assert nf4.mean() < nf2.mean()
+
+
+def test_bvh8_quantized_boxes_hold_their_bvh2_sources():
+    """Every BVH8 slot, decoded as the kernels decode it (fmaf(q, 2^exp,
+    origin) in binary32), contains the exact padded box it was quantized
+    from; the validator rejects a slot shrunk by one step."""
+    tris = scenes.random_triangles(5000, 77, mu=math.log(0.02))
+    b = BVH.build(tris)
+    info = b.info
+    assert info["bvh8_nodes"] > 0 and info["max_stack"][LAYOUT_BVH8] <= 128
+    n8, _ = b.arrays(LAYOUT_BVH8)
+    n2, _ = b.arrays(LAYOUT_BVH2)
+    assert (n8["exp"] >= -126).all()
+    step = np.ldexp(np.float32(1), n8["exp"].astype(np.int32)).astype(np.float32)  # (N, 3)
+    for axis, (lo_f, hi_f) in enumerate((("lo_x", "hi_x"), ("lo_y", "hi_y"), ("lo_z", "hi_z"))):
+        org = n8["origin"][:, axis:axis + 1]
+        s = step[:, axis:axis + 1]
+        # float32 fma: the product of a byte and a power of two is exact, so
+        # one float32 rounding of (q * s + origin) is the sum rounded once
+        dec_lo = (n8[lo_f].astype(np.float64) * s + org).astype(np.float32)
+        dec_hi = (n8[hi_f].astype(np.float64) * s + org).astype(np.float32)
+        valid = (n8["valid"][:, None] >> np.arange(8)) & 1 == 1
+        assert (dec_lo <= dec_hi)[valid].all()
+    # the root's slots hold the BVH2 root's children
+    root_lo = min(n2[0]["c0_x"][0], n2[0]["c1_x"][0])
+    assert np.float32(n8[0]["origin"][0]) == root_lo
+
+
+
+def test_bvh8_validator_rejects_a_collapsed_slot(tmp_path):
+    tris = scenes.random_triangles(3000, 78, mu=math.log(0.03))
+    b = BVH.build(tris)
+    path = os.path.join(tmp_path, "b.bvh")
+    b.save(path)
+    raw = bytearray(open(path, "rb").read())
+    n2, prims = b.arrays(LAYOUT_BVH2)
+    n4, _ = b.arrays(LAYOUT_BVH4)
+    n8, _ = b.arrays(LAYOUT_BVH8)
+    header = 8 + 4 + 4 + 8 * 8 + 96
+    off8 = (header + len(tris) * 48 + len(n2) * 64 + len(n4) * 128 + len(prims) * 48)
+    assert off8 + len(n8) * 96 + len(n8) * 32 == len(raw)
+    hi_x = off8 + 24  # node 0, slot 0
+    lo_x = off8 + 16
+    raw[hi_x] = raw[lo_x]  # slot 0 of the root collapses to one plane on x
+    open(path, "wb").write(bytes(raw))
+    with pytest.raises(IgxrtError):
+        BVH.load(path)

@@ -52,7 +52,7 @@ def test_oracle_gbuffer_encodes_hits_and_misses():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 @pytest.mark.parametrize("dims,jitter", [((61, 37), (0.5, 0.5)), ((8, 4), (0.0, 0.0)),
                                          ((130, 67), (0.123, 0.877))])
 def test_gbuffer_matches_oracle(ctx, layout, dims, jitter):

@@ -147,3 +147,18 @@ def test_gpu_build_rejects_non_finite_and_handles_empty(ctx):
     assert (empty.trace_geometry(rays)["prim"] == 0xFFFFFFFF).all()
     ok = ctx.create_scene_gpu(tris)  # the context still works
     oracle_check(ok, tris, rays, "after a rejected build")
+
+
+def test_gpu_build_has_no_bvh8(ctx):
+    """GPU builds emit BVH2 and BVH4 only; the compressed BVH8 layout is a
+    host-build layout, and tracing it on a GPU-built scene is refused."""
+    tris = scenes.random_triangles(2000, 81)
+    scene = ctx.create_scene_gpu(tris)
+    assert scene.info["bvh8_nodes"] == 0
+    saved = ctx.launch_params
+    ctx.set_launch_params(layout=2)
+    try:
+        with pytest.raises(IgxrtError):
+            scene.trace_geometry(scenes.incoherent_rays(64, 82))
+    finally:
+        ctx.set_launch_params(**saved)

@@ -118,7 +118,7 @@ def test_mixed_bvh_builds_validates_and_roundtrips(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_gpu_mixed_golden(ctx, layout):
     g, sc = golden_scene()
     saved = ctx.launch_params
@@ -132,7 +132,7 @@ def test_gpu_mixed_golden(ctx, layout):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 @pytest.mark.parametrize("seed", [3, 4])
 def test_gpu_mixed_matches_oracle(ctx, layout, seed):
     sc = random_mixed(seed)

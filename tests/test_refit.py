@@ -9,7 +9,7 @@ with a BVH the boxes must follow the geometry.  Checks:
     leaf union padded by max(2^-18 * max|coordinate|, 1e-30), interior union);
   * traversal of a refit tree equals the brute-force oracle on the moved
     geometry;
-  * the GPU refit equals the host refit bit for bit (nodes of both layouts,
+  * the GPU refit equals the host refit bit for bit (nodes of every layout,
     records), through host staging and through CUDA tensors.
 """
 import math
@@ -19,7 +19,7 @@ import pytest
 
 from conftest import NO_HIT, assert_hits_equal, bits
 from igx_raytracing_gb300 import BVH, IgxrtError, scenes
-from igx_raytracing_gb300._capi import CUBE_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, TRIANGLE_DTYPE
+from igx_raytracing_gb300._capi import CUBE_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, TRIANGLE_DTYPE
 from oracle import pyoracle
 
 
@@ -150,7 +150,7 @@ def assert_same_arrays(a, b):
 
 
 def assert_bvh_equal(x: BVH, y: BVH):
-    for layout in (LAYOUT_BVH2, LAYOUT_BVH4):
+    for layout in (LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8):
         nx, px = x.arrays(layout)
         ny, py = y.arrays(layout)
         assert_same_arrays(nx, ny)
@@ -221,7 +221,7 @@ def test_refit_traversal_matches_brute_force():
         b.refit(moved)
         expect, flags = pyoracle.trace_geometry(moved, rays)
         ok = (flags & pyoracle.EVENT_NAN_T) == 0
-        for layout in (LAYOUT_BVH2, LAYOUT_BVH4):
+        for layout in (LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8):
             nodes, prims = b.arrays(layout)
             got = pyoracle.bvh_trace(layout, nodes, prims, rays)
             assert_hits_equal(got[ok], expect["prim"][ok], expect["t"][ok], expect["u"][ok],
@@ -301,7 +301,7 @@ def test_gpu_refit_equals_host_refit(ctx, n, device_buffers):
 
 
 def assert_bvh_arrays_equal(scene, b):
-    for layout in (LAYOUT_BVH2, LAYOUT_BVH4):
+    for layout in (LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8):
         sn, sp = scene.read_bvh(layout)
         bn, bp = b.arrays(layout)
         assert_same_arrays(sn, bn)
@@ -323,7 +323,7 @@ def test_gpu_refit_traces_match_oracle(ctx):
         sh["tmax"] = np.float32(0.3)
         occ, oflags = pyoracle.trace_occlusion(moved, sh)
         ook = (oflags & pyoracle.EVENT_NAN_T) == 0
-        for layout in (LAYOUT_BVH2, LAYOUT_BVH4):
+        for layout in (LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8):
             ctx.set_launch_params(layout=layout)
             got = scene.trace_geometry(rays)
             assert_hits_equal(got[ok], expect["prim"][ok], expect["t"][ok], expect["u"][ok],

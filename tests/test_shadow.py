@@ -59,7 +59,7 @@ def test_oracle_packing_layout():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 @pytest.mark.parametrize("dims", [(37, 23, 3), (16, 2, 1), (1, 1, 2), (64, 40, 2)])
 def test_shadow_mask_matches_oracle(ctx, layout, dims):
     w, h, s = dims

@@ -7,12 +7,12 @@ import pytest
 
 from conftest import (GOLDEN_CASES, NO_HIT, assert_hits_equal, bits, closest_rays, load_golden,
                       nan_free, occlusion_rays)
-from igx_raytracing_gb300 import BVH, IgxrtError, LAYOUT_BVH2, LAYOUT_BVH4, scenes
+from igx_raytracing_gb300 import BVH, IgxrtError, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, scenes
 from igx_raytracing_gb300._capi import HIT_DTYPE, TRIANGLE_DTYPE
 from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
-LAYOUTS = [LAYOUT_BVH2, LAYOUT_BVH4]
+LAYOUTS = [LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8]
 
 
 @pytest.fixture

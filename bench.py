@@ -13,13 +13,16 @@ Workloads (seeded synthetic inputs, no dataset):
   batch         64 random-triangle scenes (1K-512K triangles, 4K-2M rays each):
                 one autotuned, graph-captured persistent launch vs 64
                 sequential plain launches.
+  serve         32 resident scenes, Poisson requests (--rate, --duration)
+                through the serving loop vs one request per launch.
 
 value: Mrays/s over all rays of a step, inputs resident in device memory,
-CUDA-event time per step (L2 flushed between steps).  e2e: the same rays
-through the C ABI with pinned host buffers (uploads and downloads inside the
-timed region).  --impl reference times the CPU transcription of the
-reference's traversal (the oracle's BVH traversal over the same BVH) on all
-host cores.
+CUDA-event time per step (L2 flushed between steps), plain kernels with the
+launch shape the engine's autotuner picks for the step.  batched: the same
+step as one graph-captured persistent launch.  e2e: the same rays through the
+C ABI with pinned host buffers (uploads and downloads inside the timed
+region).  --impl reference times the CPU transcription of the reference's
+traversal (the oracle's BVH traversal over the same BVH) on all host cores.
 """
 from __future__ import annotations
 
@@ -43,7 +46,8 @@ RAY_BYTES = 32
 HIT_BYTES = 16
 OCC_BYTES = 4
 PREV_BYTES = 4
-NODE_BYTES = {0: 64, 1: 128}
+NODE_BYTES = {0: 64, 1: 128, 2: 96}
+LAYOUT_NAMES = {0: "bvh2", 1: "bvh4", 2: "bvh8"}
 PRIM_BYTES = 48
 
 
@@ -99,14 +103,45 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def traffic_from_profiles(workload: str, batch: str):
-    """DRAM bytes per launch from a committed ncu summary, if one exists."""
-    p = os.path.join(REPO, "profiles", "dram_traffic.json")
+def traffic_from_profiles(workload: str, batch: str, layout: int):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary profiles/dram_traffic.txt: lines of
+    `<workload> <batch> <layout> <bytes>`, '#' starts a comment."""
+    p = os.path.join(REPO, "profiles", "dram_traffic.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        d = json.load(f)
-    return d.get(workload, {}).get(batch)
+        for line in f:
+            parts = line.split("#", 1)[0].split()
+            if len(parts) == 4 and parts[0] == workload and parts[1] == batch and parts[2] == LAYOUT_NAMES[layout]:
+                return int(parts[3])
+    return None
+
+
+TIMED_REGION = "igxrt_timed_region"
+
+
+def timed_region_start():
+    """NVTX start/end range around the timed steps, so a profiler can list the
+    launches of the timed region alone (ncu --nvtx --nvtx-include
+    igxrt_timed_region)."""
+    try:
+        import torch
+
+        return torch.cuda.nvtx.range_start(TIMED_REGION)
+    except Exception:
+        return None
+
+
+def timed_region_end(handle) -> None:
+    if handle is None:
+        return
+    try:
+        import torch
+
+        torch.cuda.nvtx.range_end(handle)
+    except Exception:
+        pass
 
 
 class ClockSampler:
@@ -241,7 +276,7 @@ def run_reference(args, rank: int, world: int):
     threads = pyoracle.hardware_threads()
     nodes, prims = bvh.arrays(0)
     total = sum(len(b[1]) for b in batches)
-    stride = max(1, total // 200000)
+    stride = max(1, total // 1000000)  # about a million rays per step
     times = []
     nrays = 0
     for step in range(args.warmup + args.steps):
@@ -310,6 +345,17 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    # launch shape: the engine's autotuner on this step's batches (unless a
+    # layout is forced); the plain launches below then run with it
+    items = [(scene, d_rays, d_prev, out, mode) for _, d_rays, d_prev, mode, out in dev_batches]
+    tuned = None
+    if args.layout is None and not args.no_tune:
+        t0 = time.perf_counter()
+        tuned, _ = ctx.autotune(items, reps=2, force=True)
+        tune_s = time.perf_counter() - t0
+        ctx.set_launch_params(**tuned)
+    layout = ctx.launch_params["layout"]
+
     def step(events=None):
         for i, (name, d_rays, d_prev, mode, out) in enumerate(dev_batches):
             if events is not None:
@@ -334,12 +380,14 @@ def run_engine(args, rank: int, world: int, local_rank: int):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
+    region = timed_region_start()
     wall0 = time.perf_counter()
     for s in range(args.steps):
         flush.fill_(float(s))  # evict the BVH and rays from L2 between steps
         step(ev[s])
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
+    timed_region_end(region)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
@@ -350,6 +398,28 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     # slowest rank defines the step time
     step_ms = max_over_ranks(float(launch_ms.sum(axis=1).mean()), dev)
     value = world * total_rays / (step_ms / 1e3) / 1e6
+
+    # the same step through the batched engine: all batches in one persistent,
+    # graph-captured launch (same launch shape), for the batched-vs-plain figure
+    batched = None
+    if len(dev_batches) > 1:
+        batch = ctx.create_batch(items, params=ctx.launch_params)
+        for _ in range(args.warmup):
+            batch.launch()
+        bts = []
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            batch.launch()
+            e1.record(stream)
+            e1.synchronize()
+            bts.append(e0.elapsed_time(e1))
+        ctx.sync()
+        batch.close()
+        bms = max_over_ranks(statistics.mean(bts), dev)
+        batched = {"ms_per_step": round(bms, 4), "mrays_s": round(world * total_rays / (bms / 1e3) / 1e6, 3),
+                   "over_plain": round(step_ms / bms, 3), "launches_per_step": 1}
 
     # roofline: algorithmic bytes per launch from the instrumented kernel
     peaks = measured_peaks()
@@ -367,8 +437,8 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
-                "traffic": traffic_from_profiles(cfg["workload"], dom["batch"]),
-                "kernel": f"trace_kernel<{'bvh4' if layout else 'bvh2'},{dom['mode']}> ({dom['batch']})",
+                "traffic": traffic_from_profiles(cfg["workload"], dom["batch"], layout),
+                "kernel": f"trace_kernel<{LAYOUT_NAMES[layout]},{dom['mode']}> ({dom['batch']})",
                 "peak_source": peaks["source"]}
     step_bytes = sum(b["bytes"] for b in per_batch)
 
@@ -414,7 +484,7 @@ def run_engine(args, rank: int, world: int, local_rank: int):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": dict(cfg, rays_per_step=total_rays, layout="bvh4" if layout else "bvh2",
+            "config": dict(cfg, rays_per_step=total_rays, layout=LAYOUT_NAMES[layout],
                            launch=ctx.launch_params, bvh_build_s=round(build_s, 2),
                            bvh2_nodes=info["bvh2_nodes"], sah_cost=round(info["sah_cost"], 2),
                            l2="256 MiB buffer written between timed steps",
@@ -428,6 +498,10 @@ def run_engine(args, rank: int, world: int, local_rank: int):
             "gpu_launches": args.steps * nb,
             "clocks": clk,
             "wall_s_timed_region": round(wall, 3)}
+    if tuned is not None:
+        line["config"]["launch_chosen_by"] = f"igxrt_autotune on the step's batches ({tune_s:.1f} s)"
+    if batched is not None:
+        line["batched"] = batched
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(bvh, batches, layout=0)
         line["cpu_baseline"]["linear_loop_mrays_s"] = round(linear_loop_rate(tris, batches), 6)
@@ -497,7 +571,9 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
     ctx.set_launch_params(**plain_params)
     clocks = ClockSampler(local_rank)
     clocks.start()
+    region = timed_region_start()
     bat = timed(batch.launch, args.steps)
+    timed_region_end(region)
     clk = clocks.stop()
     bat_ms = statistics.mean(bat)
     ctx.sync()
@@ -553,8 +629,8 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
             "results_equal_plain": bool(same),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
                          "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
-                         "traffic": traffic_from_profiles("batch_64_scenes_1k_512k_tris_4k_2m_rays", "batch"),
-                         "kernel": f"batch_kernel<{'bvh4' if layout else 'bvh2'}>",
+                         "traffic": traffic_from_profiles("batch_64_scenes_1k_512k_tris_4k_2m_rays", "batch", layout),
+                         "kernel": f"batch_kernel<{LAYOUT_NAMES[layout]}>",
                          "peak_source": peaks["source"]},
             "e2e": {"value": round(world * total_rays / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                     "h2d_bytes_per_step": total_rays * RAY_BYTES,
@@ -717,6 +793,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--layout", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--streams", type=int, default=2, help="serve: batches in flight")

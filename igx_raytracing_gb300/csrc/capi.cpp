@@ -51,7 +51,7 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
     if (!out.block_size)
         out.block_size = 128;
     if (!out.packet_size)
-        out.packet_size = 64;
+        out.packet_size = 32;
     if (out.stack_depth == 0 && in.block_size == 0 && in.packet_size == 0)
         out.stack_depth = 16;
     if (!out.refill_lanes)

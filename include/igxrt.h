@@ -341,11 +341,11 @@ igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info
 
 /* Launch shape of the traversal kernels. Zero fields take the defaults. */
 typedef struct igxrt_launch_params {
-    uint32_t block_size;  /* threads per CTA: 64, 128 or 256 */
-    uint32_t stack_depth; /* shared-memory stack entries per thread: 8, 16 or 32;
-                             deeper entries spill to local memory */
-    uint32_t packet_size; /* rays a warp takes per queue fetch before it starts
-                             refilling single lanes: a multiple of 32 */
+    uint32_t block_size;  /* threads per CTA: 64, 128 or 256; 0 = 128 */
+    uint32_t stack_depth; /* shared-memory stack entries per thread (at most 64);
+                             deeper entries spill to local memory; 0 = 16 */
+    uint32_t packet_size; /* rays a warp claims per queue fetch: a multiple of
+                             32 up to 4096; 0 = 32 */
     uint32_t layout;      /* IGXRT_LAYOUT_* */
     uint32_t ctas_per_sm; /* persistent CTAs per SM, 0 = as many as fit */
     uint32_t refill_lanes;/* a warp refetches rays once this many of its lanes

@@ -61,17 +61,44 @@ def bits(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
 
 
-def assert_hits_equal(got, expect_prim, expect_t, expect_u, expect_v, what=""):
-    """Bit-exact prim, t, u, v (misses: prim = NO_RAY_HIT and t = noHit)."""
-    bad = np.nonzero(got["prim"] != expect_prim)[0]
-    assert len(bad) == 0, f"{what}: {len(bad)} primitive mismatches, first rays {bad[:8]}"
+def f64_report(rays, tris, idx, got_prim, expect_prim, limit: int = 8) -> str:
+    """Re-intersects both candidate triangles of each disagreeing ray in
+    binary64 (oracle/pyoracle.reintersect_f64) and prints the result, so a
+    failure shows which side the exact arithmetic supports."""
+    from oracle import pyoracle
+
+    lines = []
+    for i in idx[:limit]:
+        parts = [f"ray {i}:"]
+        for name, p in (("got", int(got_prim[i])), ("expected", int(expect_prim[i]))):
+            if p == 0xFFFFFFFF or p >= len(tris):
+                parts.append(f"{name} miss")
+                continue
+            ok, t, u, v = pyoracle.reintersect_f64(rays[i:i + 1], tris[p:p + 1])
+            parts.append(f"{name} prim {p}: f64 {'hit' if ok else 'no hit'} t={t:.17g} u={u:.17g} v={v:.17g}")
+        lines.append(" ".join(parts))
+    text = "\n".join(lines)
+    if text:
+        print("FP64 re-intersection of disagreements:\n" + text)
+    return text
+
+
+def assert_hits_equal(got, expect_prim, expect_t, expect_u, expect_v, what="", rays=None, tris=None):
+    """Bit-exact prim, t, u, v (misses: prim = NO_RAY_HIT and t = noHit).  With
+    the rays and triangles given, every disagreement is re-intersected in
+    binary64 and logged."""
+    hit = expect_prim != 0xFFFFFFFF
+    bad_mask = got["prim"] != expect_prim
     for f, e in (("t", expect_t), ("u", expect_u), ("v", expect_v)):
-        hit = expect_prim != 0xFFFFFFFF
-        g, x = bits(got[f])[hit], bits(e)[hit]
+        g, x = bits(got[f]), bits(e)
         # NaN payloads differ between host ISAs (x86 0xffc00000, Arm 0x7fc00000)
-        both_nan = np.isnan(np.asarray(got[f])[hit]) & np.isnan(np.asarray(e)[hit])
-        nb = np.nonzero((g != x) & ~both_nan)[0]
-        assert len(nb) == 0, f"{what}: {len(nb)} {f} bit mismatches"
+        both_nan = np.isnan(np.asarray(got[f])) & np.isnan(np.asarray(e))
+        bad_mask |= hit & (g != x) & ~both_nan
+    bad = np.nonzero(bad_mask)[0]
+    if len(bad) and rays is not None and tris is not None:
+        f64_report(rays, tris, bad, got["prim"], expect_prim)
+    assert len(bad) == 0, (f"{what}: {len(bad)} rays disagree (prim {int((got['prim'] != expect_prim).sum())}),"
+                           f" first rays {bad[:8]}")
 
 
 @pytest.fixture(scope="session")

@@ -55,7 +55,7 @@ def test_cpu_bvh_matches_brute_force_random(layout):
     expect, flags = pyoracle.trace_geometry(tris, rays)
     assert not (flags & pyoracle.EVENT_NAN_T).any()
     got = pyoracle.bvh_trace(layout, nodes, prims, rays)
-    assert_hits_equal(got, expect["prim"], expect["t"], expect["u"], expect["v"], "random")
+    assert_hits_equal(got, expect["prim"], expect["t"], expect["u"], expect["v"], "random", rays=rays, tris=tris)
 
 
 def test_sphere_rays_match_brute_force():

@@ -26,7 +26,8 @@ def oracle_check(scene, tris, rays, what):
     expect, flags = pyoracle.trace_geometry(tris, rays)
     ok = (flags & pyoracle.EVENT_NAN_T) == 0
     got = scene.trace_geometry(rays)
-    assert_hits_equal(got[ok], expect["prim"][ok], expect["t"][ok], expect["u"][ok], expect["v"][ok], what)
+    assert_hits_equal(got[ok], expect["prim"][ok], expect["t"][ok], expect["u"][ok], expect["v"][ok], what,
+                      rays=rays[ok], tris=tris)
     sh = rays.copy()
     sh["tmax"] = np.float32(0.25)
     occ, oflags = pyoracle.trace_occlusion(tris, sh)

@@ -117,3 +117,24 @@ def test_golden_fixtures_are_bitwise_stable():
     hit = g["hit_prim"] != 0xFFFFFFFF
     assert set(np.unique(g["hit_prim"][hit])) <= set(range(10))
     assert (bits(g["hit_t"][~hit]) == bits(np.float32(NO_HIT))).all()
+
+
+def test_disagreements_are_reintersected_in_f64(capsys):
+    """A planted disagreement (the oracle's own answer with one primitive id
+    changed, on the CPU) fails the parity check and logs the binary64
+    re-intersection of both candidates."""
+    from conftest import assert_hits_equal
+
+    g = load_golden("heightfield")
+    rays = g["rays"].copy()
+    rays["tmin"] = 0.0
+    rays["tmax"] = NO_HIT
+    got, _ = pyoracle.trace_geometry(g["tris"], rays)
+    i = int(np.nonzero(got["prim"] != 0xFFFFFFFF)[0][0])
+    planted = got.copy()
+    planted["prim"][i] = (planted["prim"][i] + 1) % len(g["tris"])
+    with pytest.raises(AssertionError):
+        assert_hits_equal(planted, got["prim"], got["t"], got["u"], got["v"], "planted",
+                          rays=rays, tris=g["tris"])
+    out = capsys.readouterr().out
+    assert f"ray {i}:" in out and "f64 hit" in out

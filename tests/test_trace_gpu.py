@@ -32,7 +32,7 @@ def test_golden_closest_host_memory(params, case, layout):
     got = scene.trace_geometry(closest_rays(g), g["prev"])
     ok = nan_free(g)
     assert_hits_equal(got[ok], g["hit_prim"][ok], g["hit_t"][ok], g["hit_u"][ok], g["hit_v"][ok],
-                      case)
+                      case, rays=closest_rays(g)[ok], tris=g["tris"])
     occ = scene.trace_occlusion(occlusion_rays(g), g["prev"])
     ok = nan_free(g, "occlusion")
     assert np.array_equal(occ[ok], g["occluded"][ok])
@@ -66,7 +66,8 @@ def test_small_workload_all_rays_vs_brute_force(ctx):
     assert not flags.any()
     scene = ctx.create_scene(tris)
     got = scene.trace_geometry(rays)
-    assert_hits_equal(got, expect["prim"], expect["t"], expect["u"], expect["v"], "heightfield")
+    assert_hits_equal(got, expect["prim"], expect["t"], expect["u"], expect["v"], "heightfield",
+                      rays=rays, tris=tris)
 
 
 @pytest.mark.parametrize("block,depth,packet", [(32, 0, 32), (64, 8, 64), (128, 16, 64),
@@ -82,7 +83,8 @@ def test_launch_shapes_agree(params, block, depth, packet, layout):
     scene = ctx.create_scene(bvh=b)
     ctx.set_launch_params(block_size=block, stack_depth=depth, packet_size=packet, layout=layout)
     got = scene.trace_geometry(rays)
-    assert_hits_equal(got, expect["prim"], expect["t"], expect["u"], expect["v"], "shape")
+    assert_hits_equal(got, expect["prim"], expect["t"], expect["u"], expect["v"], "shape",
+                      rays=rays, tris=tris)
     sh = rays.copy()
     sh["tmax"] = 0.05
     assert np.array_equal(scene.trace_occlusion(sh),

@@ -113,12 +113,21 @@ __device__ __forceinline__ bool tri_test(const RayState& r, const float4& v0, co
     const float hx = __fsub_rn(__fmul_rn(r.dy, v2.z), __fmul_rn(v2.y, r.dz));
     const float hy = __fsub_rn(__fmul_rn(r.dz, v2.x), __fmul_rn(v2.z, r.dx));
     const float hz = __fsub_rn(__fmul_rn(r.dx, v2.y), __fmul_rn(v2.x, r.dy));
-    // a = dot(e1, h); f = 1 / a
+    // a = dot(e1, h); s = pos - p0; dsh = dot(s, h)
     const float a = __fadd_rn(__fadd_rn(__fmul_rn(v1.x, hx), __fmul_rn(v1.y, hy)), __fmul_rn(v1.z, hz));
-    const float f = __frcp_rn(a);
-    // s = pos - p0; u = f * dot(s, h)
     const float sx = __fsub_rn(r.ox, v0.x), sy = __fsub_rn(r.oy, v0.y), sz = __fsub_rn(r.oz, v0.z);
-    u = __fmul_rn(f, __fadd_rn(__fadd_rn(__fmul_rn(sx, hx), __fmul_rn(sy, hy)), __fmul_rn(sz, hz)));
+    const float dsh = __fadd_rn(__fadd_rn(__fmul_rn(sx, hx), __fmul_rn(sy, hy)), __fmul_rn(sz, hz));
+    // u = f * dsh with f = 1/a rounded has the sign of a * dsh; it is < 0
+    // (rejected below) whenever the signs differ, dsh != 0, a is finite and
+    // |dsh| >= 2^-100 |a|, since then |u| >= 2^-100 (1 - 2^-24) cannot round
+    // to zero (for a = 0, f is infinite and u = -inf).  Deciding that case
+    // before the correctly rounded reciprocal changes no result.
+    if (((__float_as_uint(a) ^ __float_as_uint(dsh)) & 0x80000000u) && dsh != 0.f &&
+        fabsf(a) <= 3.4028235e38f && __fmul_rn(fabsf(dsh), 0x1p100f) >= fabsf(a))
+        return false;
+    // f = 1 / a; u = f * dot(s, h)
+    const float f = __frcp_rn(a);
+    u = __fmul_rn(f, dsh);
     if (u < 0.f || u > 1.f)
         return false;
     // q = cross(s, e1); v = f * dot(dir, q)

@@ -15,6 +15,14 @@ Workloads (seeded synthetic inputs, no dataset):
                 sequential plain launches.
   serve         32 resident scenes, Poisson requests (--rate, --duration)
                 through the serving loop vs one request per launch.
+  gbuffer       the sphere's 1080p raygen pass as one kernel (rays, hits,
+                dirObject / uvNormal encodings) vs camera rays + plain trace.
+  shadowmask    the sphere's shadow pass packed into ballot words vs plain
+                any-hit on the same rays.
+  mixed         1M triangles + 64K spheres + 64K cubes + 4 planes, 4M
+                incoherent rays.
+  dynamic       the sphere deforming every frame: refit + 1080p primaries
+                per step, beside a GPU rebuild per frame.
 
 value: Mrays/s over all rays of a step, inputs resident in device memory,
 CUDA-event time per step (L2 flushed between steps), plain kernels with the
@@ -783,13 +791,337 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------
+# The passes beside the plain queries: shadow mask, G-buffer, mixed
+# primitives, moving geometry
+# --------------------------------------------------------------------------
+
+def _event_ms(torch, fn, steps: int, flush, stream) -> list:
+    """CUDA-event time of fn() per step, L2 flushed before each."""
+    ts = []
+    region = timed_region_start()
+    for s in range(steps):
+        flush.fill_(float(s))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    timed_region_end(region)
+    return ts
+
+
+def _line(args, world, value, ms, cfg, **extra) -> dict:
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg}
+    line.update(extra)
+    return line
+
+
+def _roofline(achieved_bytes: int, ms: float, kernel: str, traffic=None) -> dict:
+    peaks = measured_peaks()
+    gbs = achieved_bytes / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": round(gbs, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(gbs / peaks["hbm_gbs"], 4), "traffic": traffic, "kernel": kernel,
+            "peak_source": peaks["source"], "bytes_per_launch": int(achieved_bytes)}
+
+
+def run_pass_bench(args, rank: int, world: int, local_rank: int):
+    """--workload gbuffer | shadowmask on the 1M-triangle sphere at 1080p.
+
+    gbuffer: igxrt_trace_gbuffer, the reference's raygen.comp as one kernel
+    (camera rays, closest hit, dirObject and uvNormal encodings); compared
+    with igxrt_camera_rays + igxrt_trace_closest (no encodings).
+    shadowmask: igxrt_trace_shadow_mask, nv_all.shadow.comp's any-hit rays
+    toward the point light packed into ballot words (one sample); compared
+    with igxrt_trace_any on the same rays (one word per ray)."""
+    import torch
+
+    import igx_raytracing_gb300 as igx
+    from igx_raytracing_gb300 import BVH, scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    ctx = igx.Context(local_rank)
+    tris, _ = scenes.workload_sphere_primary()
+    bvh = BVH.build(tris)
+    scene = ctx.create_scene(bvh=bvh)
+    w, h = 1920, 1080
+    cam = scenes.camera_record(w, h, eye=(0.0, -3.0, 0.0), target=(0.0, 0.0, 0.0))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    rays = ctx.camera_rays(cam)
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+    hits_h = ctx.trace_closest(scene, rays)
+    hit = hits_h["prim"] != 0xFFFFFFFF
+    layout = ctx.launch_params["layout"]
+    cfg = {"triangles": len(tris), "width": w, "height": h, "layout": LAYOUT_NAMES[layout],
+           "launch": ctx.launch_params, "l2": "256 MiB buffer written between timed steps"}
+
+    if args.workload == "gbuffer":
+        d_do = torch.empty((h, w, 4), dtype=torch.float32, device=dev)
+        d_uv = torch.zeros((h, w, 4), dtype=torch.float32, device=dev)
+        fused = lambda: ctx.trace_gbuffer(scene, cam, d_do, d_uv)
+        d_hits = torch.empty((w * h, 4), dtype=torch.float32, device=dev)
+        split = lambda: (ctx.camera_rays(cam, out=d_rays), ctx.trace_closest(scene, d_rays, out=d_hits))
+        for _ in range(args.warmup):
+            fused()
+            split()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local_rank)
+        clocks.start()
+        ms = statistics.mean(_event_ms(torch, fused, args.steps, flush, stream))
+        clk = clocks.stop()
+        split_ms = statistics.mean(_event_ms(torch, split, args.steps, flush, stream))
+        nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
+        # per pixel: dirObject written (16 B); on a hit also uvNormal (16 B) and
+        # the hit triangle's normals (48 B); no ray is read
+        b = int(16 * len(rays) + (16 + 48) * int(hit.sum()) + NODE_BYTES[layout] * int(nf.sum(dtype=np.int64))
+                + PRIM_BYTES * int(pf.sum(dtype=np.int64)))
+        hdo = np.empty((h, w, 4), np.float32)
+        huv = np.empty((h, w, 4), np.float32)
+        ctx.trace_gbuffer(scene, cam, hdo, huv)
+        e2e = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            ctx.trace_gbuffer(scene, cam, hdo, huv)
+            e2e.append(time.perf_counter() - t0)
+        e2e_ms = 1000 * statistics.mean(e2e)
+        n = w * h
+        line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,
+                     dict(cfg, workload="gbuffer_sphere_1m_1080p", rays_per_step=n),
+                     roofline=_roofline(b, ms, f"gbuffer_kernel<{LAYOUT_NAMES[layout]}>"),
+                     e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
+                          "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 32 * n,
+                          "ms_per_step": round(e2e_ms, 3)},
+                     split={"ms_per_step": round(split_ms, 4),
+                            "mrays_s": round(n / (split_ms / 1e3) / 1e6, 3),
+                            "what": "igxrt_camera_rays + igxrt_trace_closest (hits, no encodings)",
+                            "fused_over_split": round(split_ms / ms, 3)},
+                     gpu_launches=args.steps, clocks=clk)
+    else:
+        # one shadow ray per pixel toward the light from the primary hit;
+        # missed pixels cast none (their ray words are never read)
+        prim = rays.copy()
+        bounce, shadow, prev = scenes.secondary_rays(tris, prim, hits_h, scenes.SPHERE_LIGHT,
+                                                     scenes.seed_for(2, 50))
+        pix_rays = np.zeros(w * h, dtype=igx.RAY_DTYPE)
+        pix_rays[hit] = shadow
+        obj = hits_h["prim"].astype(np.uint32)
+        d_pix = torch.from_numpy(pix_rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+        d_obj = torch.from_numpy(obj.view(np.int32).copy()).to(dev)
+        words = ((w + 15) // 16) * ((h + 1) // 2)
+        d_mask = torch.empty(words, dtype=torch.int32, device=dev)
+        d_sh = torch.from_numpy(shadow.view(np.float32).reshape(-1, 8).copy()).to(dev)
+        d_prev = torch.from_numpy(prev.view(np.int32).copy()).to(dev)
+        d_occ = torch.empty(len(shadow), dtype=torch.int32, device=dev)
+        fused = lambda: ctx.trace_shadow_mask(scene, d_pix, d_obj, w, h, 1, out=d_mask)
+        plain = lambda: ctx.trace_any(scene, d_sh, d_prev, out=d_occ)
+        for _ in range(args.warmup):
+            fused()
+            plain()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local_rank)
+        clocks.start()
+        ms = statistics.mean(_event_ms(torch, fused, args.steps, flush, stream))
+        clk = clocks.stop()
+        plain_ms = statistics.mean(_event_ms(torch, plain, args.steps, flush, stream))
+        nf, pf = ctx.count_fetches(scene, shadow, prev, mode=1, layout=layout)
+        # per traced ray: ray (32 B) + its pixel's object (4 B, the prevHit);
+        # every pixel's object word is read, every mask word written
+        n = int(hit.sum())
+        b = int(32 * n + 4 * w * h + 4 * words + NODE_BYTES[layout] * int(nf.sum(dtype=np.int64))
+                + PRIM_BYTES * int(pf.sum(dtype=np.int64)))
+        hmask = np.empty(words, np.uint32)
+        ctx.trace_shadow_mask(scene, pix_rays, obj, w, h, 1, out=hmask)
+        e2e = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            ctx.trace_shadow_mask(scene, pix_rays, obj, w, h, 1, out=hmask)
+            e2e.append(time.perf_counter() - t0)
+        e2e_ms = 1000 * statistics.mean(e2e)
+        line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,
+                     dict(cfg, workload="shadowmask_sphere_1m_1080p_1_sample", rays_per_step=n,
+                          light=list(scenes.SPHERE_LIGHT)),
+                     roofline=_roofline(b, ms, f"shadow_mask_kernel<{LAYOUT_NAMES[layout]}>"),
+                     e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
+                          "h2d_bytes_per_step": 36 * w * h, "d2h_bytes_per_step": 4 * words,
+                          "ms_per_step": round(e2e_ms, 3)},
+                     plain={"ms_per_step": round(plain_ms, 4),
+                            "mrays_s": round(n / (plain_ms / 1e3) / 1e6, 3),
+                            "what": "igxrt_trace_any on the same rays (one word per ray, no packing)"},
+                     gpu_launches=args.steps, clocks=clk)
+    if rank == 0:
+        if world == 1 and not args.no_cpu_baseline:
+            mode = 0 if args.workload == "gbuffer" else 1
+            sample = [("camera" if mode == 0 else "shadow", rays if mode == 0 else shadow,
+                       None if mode == 0 else prev, mode)]
+            line["cpu_baseline"] = cpu_baseline(bvh, sample, layout=0)
+        print(json.dumps(line), flush=True)
+
+
+def run_mixed_bench(args, rank: int, world: int, local_rank: int):
+    """--workload mixed: 1M triangles, 64K spheres, 64K cubes and 4 planes
+    (the reference's four primitive types, trace.glsl:22-46) in one tree,
+    4M incoherent rays, closest hit."""
+    import torch
+
+    import igx_raytracing_gb300 as igx
+    from igx_raytracing_gb300 import BVH, scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    ctx = igx.Context(local_rank)
+    sc = scenes.workload_mixed()
+    rays = scenes.incoherent_rays(4_194_304, scenes.seed_for(6, 1))
+    t0 = time.perf_counter()
+    bvh = BVH.build_mixed(sc["tris"], sc["spheres"], sc["cubes"], sc["planes"])
+    build_s = time.perf_counter() - t0
+    scene = ctx.create_scene(bvh=bvh)
+    layout = ctx.launch_params["layout"]
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+    out = torch.empty((len(rays), 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    fn = lambda: ctx.trace_closest(scene, d_rays, out=out)
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms = statistics.mean(_event_ms(torch, fn, args.steps, flush, stream))
+    clk = clocks.stop()
+    nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
+    planes = len(sc["planes"])
+    b = algorithmic_bytes(nf, pf, 0, False, layout) + 16 * planes * len(rays)
+    hrays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory().numpy().view(igx.RAY_DTYPE).reshape(-1)
+    hout = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory().numpy().view(igx.HIT_DTYPE).reshape(-1)
+    ctx.trace_closest(scene, hrays, out=hout)
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.trace_closest(scene, hrays, out=hout)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = 1000 * statistics.mean(e2e)
+    n = len(rays)
+    cfg = {"workload": "mixed_1m_tris_64k_spheres_64k_cubes_4_planes_4m_incoherent",
+           "triangles": len(sc["tris"]), "spheres": len(sc["spheres"]), "cubes": len(sc["cubes"]),
+           "planes": planes, "rays_per_step": n, "layout": LAYOUT_NAMES[layout],
+           "launch": ctx.launch_params, "bvh_build_s": round(build_s, 2),
+           "l2": "256 MiB buffer written between timed steps"}
+    line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms, cfg,
+                 roofline=_roofline(b, ms, f"trace_kernel<{LAYOUT_NAMES[layout]},closest,mixed>"),
+                 e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
+                      "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 16 * n,
+                      "ms_per_step": round(e2e_ms, 3)},
+                 fetches={"nodes_per_ray": round(float(nf.mean()), 3), "prims_per_ray": round(float(pf.mean()), 3)},
+                 gpu_launches=args.steps, clocks=clk)
+    if rank == 0:
+        if world == 1 and not args.no_cpu_baseline:
+            from oracle import pyoracle
+
+            sample = rays[:: max(1, n // 64)][:64]
+            t0 = time.perf_counter()
+            pyoracle.trace_geometry_mixed(sample, None, **sc)
+            dt = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": round(len(sample) / dt / 1e6, 6), "unit": UNIT,
+                                    "cores": pyoracle.hardware_threads(), "kind": "port",
+                                    "sample": f"{len(sample)} rays through the oracle's linear loop over all "
+                                              "objects (the reference's trace.glsl:22-46 order)"}
+        print(json.dumps(line), flush=True)
+
+
+def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
+    """--workload dynamic: the 1M-triangle sphere deforms every frame (the
+    reference re-uploads moving geometry per frame, niels_scene.cpp:61-70).
+    A step is one frame: new positions (device-resident) -> igxrt_scene_refit
+    -> 1080p primaries.  Beside it: the same frame with a full GPU rebuild
+    (igxrt_scene_create_gpu) instead of the refit."""
+    import torch
+
+    import igx_raytracing_gb300 as igx
+    from igx_raytracing_gb300 import BVH, scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    ctx = igx.Context(local_rank)
+    tris, rays = scenes.workload_sphere_primary()
+    frames = []
+    for k in range(4):  # a breathing, twisting sphere
+        f = tris.copy()
+        for v in ("p0", "p1", "p2"):
+            p = f[v].astype(np.float64)
+            s = 1.0 + 0.05 * math.sin(0.7 * k) * np.sin(3.0 * p[:, 2] + k)
+            f[v] = (p * s[:, None]).astype(np.float32)
+        frames.append(torch.from_numpy(f.view(np.float32).reshape(-1, 12).copy()).to(dev))
+    t0 = time.perf_counter()
+    bvh = BVH.build(tris)
+    host_build_s = time.perf_counter() - t0
+    scene = ctx.create_scene(bvh=bvh)
+    layout = ctx.launch_params["layout"]
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
+    out = torch.empty((len(rays), 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    counter = {"k": 0}
+
+    def refit_frame():
+        scene.refit(frames[counter["k"] % len(frames)])
+        counter["k"] += 1
+        ctx.trace_closest(scene, d_rays, out=out)
+
+    def rebuild_frame():
+        g = ctx.create_scene_gpu(frames[counter["k"] % len(frames)])
+        counter["k"] += 1
+        ctx.trace_closest(g, d_rays, out=out)
+        torch.cuda.synchronize()
+        g.close()
+
+    for _ in range(args.warmup):
+        refit_frame()
+        rebuild_frame()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms = statistics.mean(_event_ms(torch, refit_frame, args.steps, flush, stream))
+    clk = clocks.stop()
+    refit_only = statistics.mean(_event_ms(torch, lambda: scene.refit(frames[0]), args.steps, flush, stream))
+    trace_only = statistics.mean(_event_ms(torch, lambda: ctx.trace_closest(scene, d_rays, out=out),
+                                           args.steps, flush, stream))
+    rebuild_ms = statistics.mean(_event_ms(torch, rebuild_frame, args.steps, flush, stream))
+    nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
+    n = len(rays)
+    b = algorithmic_bytes(nf, pf, 0, False, layout)
+    cfg = {"workload": "dynamic_sphere_1m_refit_1080p_primary", "triangles": len(tris),
+           "rays_per_step": n, "layout": LAYOUT_NAMES[layout], "launch": ctx.launch_params,
+           "frames": len(frames), "host_sah_build_s": round(host_build_s, 3),
+           "l2": "256 MiB buffer written between timed steps"}
+    line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms, cfg,
+                 roofline=_roofline(b, trace_only, f"trace_kernel<{LAYOUT_NAMES[layout]},closest> (frame rays)"),
+                 frame={"refit_ms": round(refit_only, 4), "trace_ms": round(trace_only, 4),
+                        "refit_plus_trace_ms": round(ms, 4),
+                        "gpu_rebuild_plus_trace_ms": round(rebuild_ms, 4),
+                        "frames_per_s_refit": round(1e3 / ms, 1),
+                        "frames_per_s_gpu_rebuild": round(1e3 / rebuild_ms, 1)},
+                 e2e={"value": round(world * n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
+                      "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0, "ms_per_step": round(ms, 4),
+                      "note": "positions and rays resident: a frame's geometry arrives from a device kernel"},
+                 gpu_launches=args.steps * 4, clocks=clk)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="sphere",
-                    choices=["sphere", "small", "incoherent", "incoherent1m", "batch", "serve"])
+                    choices=["sphere", "small", "incoherent", "incoherent1m", "batch", "serve",
+                             "gbuffer", "shadowmask", "mixed", "dynamic"])
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--layout", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -814,6 +1146,12 @@ def main():
         run_batch_bench(args, rank, world, local_rank)
     elif args.workload == "serve":
         run_serve_bench(args, rank, world, local_rank)
+    elif args.workload in ("gbuffer", "shadowmask"):
+        run_pass_bench(args, rank, world, local_rank)
+    elif args.workload == "mixed":
+        run_mixed_bench(args, rank, world, local_rank)
+    elif args.workload == "dynamic":
+        run_dynamic_bench(args, rank, world, local_rank)
     else:
         run_engine(args, rank, world, local_rank)
     if world > 1:

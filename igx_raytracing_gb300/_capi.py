@@ -222,6 +222,7 @@ assert CAMERA_DTYPE.itemsize == 64
 
 PROTOTYPES += [
     ("igxrt_trace_gbuffer", _st, [_vp, _vp, _vp, _vp, _vp, _u32, _vp]),
+    ("igxrt_camera_rays", _st, [_vp, _vp, _vp, _u32, _vp]),
 ]
 
 # igxrt_cube (24 bytes) and igxrt_scene_desc

@@ -475,6 +475,21 @@ class Context:
               "gbuffer")
         return dir_object, uv_normal
 
+    def camera_rays(self, camera, out=None, stream=None):
+        """igxrt_camera_rays: the G-buffer pass's primary rays in pixel order
+        (numpy RAY_DTYPE, or into `out`, an (n, 8) float32 CUDA tensor)."""
+        cam = np.ascontiguousarray(camera, dtype=_capi.CAMERA_DTYPE).reshape(1)
+        n = int(cam["width"][0]) * int(cam["height"][0])
+        fn = lib().igxrt_camera_rays
+        if out is not None and _is_cuda_tensor(out):
+            check(fn(self._h, cam.ctypes.data, out.data_ptr(), 0, self._stream(stream, True)), self._h,
+                  "camera_rays")
+            return out
+        rays = np.zeros(n, dtype=RAY_DTYPE)
+        check(fn(self._h, cam.ctypes.data, rays.ctypes.data if n else None, TRACE_HOST_MEMORY,
+                 self._stream(stream, False)), self._h, "camera_rays")
+        return rays
+
     def count_fetches(self, scene: Scene, rays, prev_hit=None, mode: int = 0,
                       layout: int = LAYOUT_BVH2):
         """Node and primitive records the kernel fetches per ray (host arrays)."""

@@ -581,8 +581,6 @@ igxrt_status igxrt_count_fetches(igxrt_context* ctx, const igxrt_scene* scene, c
         return IGXRT_ERROR_INVALID_ARGUMENT;
     if (mode > 1 || layout >= IGXRT_LAYOUT_COUNT || !node_fetches || !prim_fetches)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "mode 0/1, a valid layout and both count arrays");
-    if (scene && scene->mixed)
-        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "fetch counts are kept for triangle-only scenes");
     if (count == 0)
         return IGXRT_OK;
     // The instrumented kernel also writes the query's results; they go to a

@@ -58,6 +58,33 @@ __device__ __forceinline__ uint2 encode_normal(float3 n) {
     return make_uint2((hx << 16) | hy, hz);
 }
 
+// calculatePrimary / calculateScreen (camera.glsl:72-87, 113-116): the unit
+// direction of pixel (x, y), every operation rounded separately.
+__device__ __forceinline__ float3 camera_dir(const igxrt_camera& c, float inv_w, float inv_h, uint32_t x,
+                                             uint32_t y) {
+    const float cx = __fmul_rn(__fadd_rn((float)x, c.jitter_x), inv_w);
+    const float cy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn((float)y, c.jitter_y), inv_h));
+    float d[3];
+    for (int k = 0; k < 3; ++k) {
+        const float right = __fsub_rn(c.p1[k], c.p0[k]), up = __fsub_rn(c.p2[k], c.p0[k]);
+        const float pos = __fadd_rn(__fadd_rn(c.p0[k], __fmul_rn(cx, right)), __fmul_rn(cy, up));
+        d[k] = __fsub_rn(pos, c.eye[k]);
+    }
+    const float len = __fsqrt_rn(dot3(d[0], d[1], d[2], d[0], d[1], d[2]));
+    return make_float3(__fdiv_rn(d[0], len), __fdiv_rn(d[1], len), __fdiv_rn(d[2], len));
+}
+
+// The primary rays of igxrt_trace_gbuffer as records: {eye, 0, dir, noHit}.
+__global__ void camera_rays_kernel(igxrt_camera c, float inv_w, float inv_h, float4* rays) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= (uint64_t)c.width * c.height)
+        return;
+    const uint32_t y = (uint32_t)(i / c.width), x = (uint32_t)(i - (uint64_t)y * c.width);
+    const float3 d = camera_dir(c, inv_w, inv_h, x, y);
+    rays[2 * i] = make_float4(c.eye[0], c.eye[1], c.eye[2], 0.f);
+    rays[2 * i + 1] = make_float4(d.x, d.y, d.z, IGXRT_NO_HIT);
+}
+
 template <int LAYOUT>
 __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
     extern __shared__ uint32_t smem[];
@@ -74,17 +101,8 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
         const uint32_t x = tx * 8u + (lane & 7u), y = ty * 4u + (lane >> 3);
         if (x >= c.width || y >= c.height)
             continue;
-        // calculatePrimary / calculateScreen
-        const float cx = __fmul_rn(__fadd_rn((float)x, c.jitter_x), a.inv_w);
-        const float cy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn((float)y, c.jitter_y), a.inv_h));
-        float d[3];
-        for (int k = 0; k < 3; ++k) {
-            const float right = __fsub_rn(c.p1[k], c.p0[k]), up = __fsub_rn(c.p2[k], c.p0[k]);
-            const float pos = __fadd_rn(__fadd_rn(c.p0[k], __fmul_rn(cx, right)), __fmul_rn(cy, up));
-            d[k] = __fsub_rn(pos, c.eye[k]);
-        }
-        const float len = __fsqrt_rn(dot3(d[0], d[1], d[2], d[0], d[1], d[2]));
-        const float dx = __fdiv_rn(d[0], len), dy = __fdiv_rn(d[1], len), dz = __fdiv_rn(d[2], len);
+        const float3 dir = camera_dir(c, a.inv_w, a.inv_h, x, y);
+        const float dx = dir.x, dy = dir.y, dz = dir.z;
         RayState r;
         r.ox = c.eye[0];
         r.oy = c.eye[1];
@@ -223,5 +241,49 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
             return cuda_fail(ctx, e, "g-buffer download");
         return read_status(ctx);
     }
+    return IGXRT_OK;
+}
+
+extern "C" igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera* cam, igxrt_ray* rays,
+                                          uint32_t flags, void* stream_ptr) {
+    if (!ctx)
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    if (!cam || !rays)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "camera and rays must be non-NULL");
+    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    const uint64_t pixels = (uint64_t)cam->width * cam->height;
+    if (!pixels)
+        return IGXRT_OK;
+    if (pixels > 0x7fffffffu || cam->width > (1u << 24) || cam->height > (1u << 24))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "image too large");
+    if ((uintptr_t)rays % 16)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "rays must be 16-byte aligned");
+    const bool host = flags & IGXRT_TRACE_HOST_MEMORY;
+    if (!host && !device_accessible(rays))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    "rays is not device memory: pass IGXRT_TRACE_HOST_MEMORY for a host array");
+    DeviceGuard guard(ctx->device);
+    if (!guard.ok())
+        return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    const size_t bytes = pixels * sizeof(igxrt_ray);
+    float4* d_rays = reinterpret_cast<float4*>(rays);
+    if (host) {
+        igxrt_status st = grow_stage(ctx, bytes);
+        if (st != IGXRT_OK)
+            return st;
+        d_rays = static_cast<float4*>(ctx->d_stage);
+    }
+    camera_rays_kernel<<<(uint32_t)((pixels + 255) / 256), 256, 0, stream>>>(
+        *cam, 1.0f / (float)cam->width, 1.0f / (float)cam->height, d_rays);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && host) {
+        e = cudaMemcpyAsync(rays, d_rays, bytes, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(stream);
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "camera rays");
     return IGXRT_OK;
 }

@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
             bool occluded = occluded_at_start;
             // leaf phase
             if (next < 0) {
-                occluded = MIXED ? process_leaf_mixed<ANY>(a.prims, next, r, best)
+                occluded = MIXED ? process_leaf_mixed<ANY, COUNT>(a.prims, next, r, best, &pf)
                                  : process_leaf<ANY, COUNT>(a.prims, next, r, best, pf);
                 if (!occluded)
                     next = st.pop_live(best.tcull);
@@ -160,11 +160,18 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
 
 using KernelFn = void (*)(KernelArgs);
 
-// Instrumented variants exist for triangle-only scenes; mixed scenes have
-// no host traversal to compare counts with.
+// Every variant has an instrumented twin (COUNT) that also writes per-ray
+// fetch counts; for triangle-only scenes they equal the host traversal's.
 static KernelFn select_kernel(uint32_t layout, bool any, bool count, bool mixed) {
     constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
     if (mixed) {
+        if (count) {  // instrumented mixed kernels: no host traversal to compare with
+            if (layout == B8)
+                return any ? trace_kernel<B8, true, true, true> : trace_kernel<B8, false, true, true>;
+            if (layout == B4)
+                return any ? trace_kernel<B4, true, true, true> : trace_kernel<B4, false, true, true>;
+            return any ? trace_kernel<B2, true, true, true> : trace_kernel<B2, false, true, true>;
+        }
         if (layout == B8)
             return any ? trace_kernel<B8, true, false, true> : trace_kernel<B8, false, false, true>;
         if (layout == B4)

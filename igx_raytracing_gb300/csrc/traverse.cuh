@@ -574,13 +574,15 @@ __device__ __forceinline__ void plane_uv(const RayState& r, const float4& pl, fl
 }
 
 // Leaf of a mixed scene.  Returns true when an any-hit query is decided.
-template <bool ANY>
+template <bool ANY, bool COUNT = false>
 __device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ prims, int32_t ref,
-                                                   const RayState& r, BestHit& best) {
+                                                   const RayState& r, BestHit& best, uint32_t* pf = nullptr) {
     uint32_t i = (uint32_t)~ref;
     for (;;) {
         const float4* p = prims + 3 * (size_t)i;
         const float4 v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
+        if (COUNT)
+            ++*pf;
         const uint32_t type = __float_as_uint(v2.w), id = __float_as_uint(v0.w);
         if (id != r.prev) {
             if (type == kPrimTriangle) {

@@ -264,6 +264,30 @@ def workload_incoherent(ntris: int = 2_097_152, nrays: int = 4_194_304, variant:
     return tris, rays
 
 
+def workload_mixed(ntris: int = 1_048_576, nspheres: int = 65_536, ncubes: int = 65_536,
+                   nplanes: int = 4) -> dict:
+    """All four of the reference's primitive types at scale, in the unit cube:
+    random triangles as workload_incoherent, spheres with radius log-normal
+    around 0.004, axis-aligned cubes with edges log-normal around 0.006, and
+    planes bounding the cube from below and the sides (normals pointing in)."""
+    from ._capi import CUBE_DTYPE
+
+    rng = np.random.default_rng(seed_for(6))
+    tris = random_triangles(ntris, seed_for(6, 1))
+    c = rng.uniform(0.0, 1.0, (nspheres, 3))
+    r = np.exp(rng.normal(math.log(0.004), 0.5, (nspheres, 1)))
+    spheres = np.concatenate([c, r], axis=1).astype(np.float32)
+    lo = rng.uniform(0.0, 1.0, (ncubes, 3))
+    hi = lo + np.exp(rng.normal(math.log(0.006), 0.5, (ncubes, 3)))
+    cubes = np.zeros(ncubes, CUBE_DTYPE)
+    cubes["xy0"] = lo[:, :2]
+    cubes["z0_x1"] = np.stack([lo[:, 2], hi[:, 0]], axis=1)
+    cubes["yz1"] = hi[:, 1:]
+    base = [(0.0, 0.0, 1.0, 0.05), (1.0, 0.0, 0.0, 0.05), (-1.0, 0.0, 0.0, -1.05), (0.0, 1.0, 0.0, 0.05)]
+    planes = np.asarray(base[:nplanes], dtype=np.float32).reshape(-1, 4)
+    return dict(tris=tris, spheres=spheres, cubes=cubes, planes=planes)
+
+
 def log_uniform_ints(rng: np.random.Generator, lo: int, hi: int, n: int) -> np.ndarray:
     return np.exp(rng.uniform(math.log(lo), math.log(hi), n)).astype(np.int64)
 

@@ -577,6 +577,13 @@ typedef struct igxrt_camera {
 igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scene* scene,
                                  const igxrt_camera* camera, float* dir_object, float* uv_normal,
                                  uint32_t flags, void* stream);
+/* The primary rays igxrt_trace_gbuffer traces, written as width*height ray
+ * records {eye, 0, dir, IGXRT_NO_HIT} in pixel order (the same binary32
+ * steps), so the pass can be split into ray generation and
+ * igxrt_trace_closest.  rays is device memory, or host memory with
+ * IGXRT_TRACE_HOST_MEMORY. */
+igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera* camera, igxrt_ray* rays,
+                               uint32_t flags, void* stream);
 
 /* Copies `count` device hits to host memory and waits for them. */
 igxrt_status igxrt_fetch_hits(igxrt_context* ctx, const igxrt_hit* device_hits,

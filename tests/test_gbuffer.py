@@ -86,3 +86,24 @@ def test_gbuffer_device_memory(ctx):
     torch.cuda.synchronize()
     assert np.array_equal(bits(d_do.cpu().numpy()), bits(e_do))
     assert np.array_equal(bits(d_uv.cpu().numpy()), bits(e_uv))
+
+
+@pytest.mark.gpu
+def test_camera_rays_split_the_gbuffer_pass(ctx):
+    """igxrt_camera_rays + igxrt_trace_closest reproduce the fused pass's
+    dir_object image bit for bit (hits: dir * t and the object id; misses:
+    the direction and noRayHit)."""
+    tris = normals_scene()
+    w, h = 67, 41
+    cam = scenes.camera_record(w, h, eye=(0.5, -1.2, 0.6), target=(0.5, 0.5, 0.45), jitter=(0.3, 0.7))
+    scene = ctx.create_scene(tris)
+    g_do, _ = ctx.trace_gbuffer(scene, cam)
+    rays = ctx.camera_rays(cam)
+    assert (rays["org"] == rays["org"][0]).all() and (rays["tmin"] == 0).all()
+    hits = ctx.trace_closest(scene, rays)
+    d = rays["dir"].astype(np.float32)
+    hit = hits["prim"] != 0xFFFFFFFF
+    expect = np.zeros((w * h, 4), np.float32)
+    expect[:, :3] = np.where(hit[:, None], d * hits["t"][:, None].astype(np.float32), d)
+    expect[:, 3] = hits["prim"].view(np.float32)
+    assert np.array_equal(bits(g_do.reshape(-1, 4)), bits(expect))

@@ -165,15 +165,23 @@ class ClockSampler:
         self.path = os.path.join(REPO, "gpurun_out", f"clocks_dev{device}.csv")
 
     def start(self):
+        """Starts sampling every 20 ms and returns once the first sample is in,
+        so even a short timed region that follows is covered."""
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                 "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.fh,
                 stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self) -> dict:
         if self.proc is None:

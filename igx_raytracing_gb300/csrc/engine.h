@@ -91,6 +91,9 @@ struct TraceRequest {
     uint32_t* occluded;
     uint32_t* node_fetches;  // non-null: instrumented kernel
     uint32_t* prim_fetches;
+    // non-null: the number of rays is this device word (written by an earlier
+    // kernel on the stream), at most `count`, which sizes the launch
+    const uint32_t* count_dev = nullptr;
 };
 
 // Records `msg` as the context's last error and returns `st`.

@@ -1,69 +1,85 @@
-// shadow.cu — the reference's shadow pass as one kernel: any-hit rays per
-// pixel and sample, packed into its 32-bit ballot words.
+// shadow.cu — the reference's shadow pass: any-hit rays per pixel and sample,
+// packed into its 32-bit ballot words.
 //
 // res/shaders/nv_all.shadow.comp:50-142 runs one thread per pixel and sample
 // in 16x16x2 work groups; on NVIDIA each 32-lane subgroup covers a 16x2 pixel
 // tile of one sample, traces traceOcclusion for pixels whose primary object
 // is not noRayHit (:108-126), and lane 0 stores ballotARB(hit) at
 // indexToLight(loc, res, sample, shift = (4,1), mask = (15,1))
-// (light.glsl:221-229).  Here a warp owns one tile word: lane l handles pixel
-// (16*tx + (l & 15), 2*ty + (l >> 4)), so the warp's ballot is that word
-// directly and the traversal of the 32 rays of a tile (neighbouring pixels,
-// one light) stays coherent.
+// (light.glsl:221-229).  A thread per pixel leaves every lane of a pixel
+// that missed the scene idle; here the pass runs in three kernels:
+//   1. compact: the (sample, pixel) pairs whose object is not noRayHit get a
+//      slot (one warp-aggregated atomicAdd per warp); their ray and object
+//      (the prevHit) are gathered into the slot, and the pair remembers its
+//      slot;
+//   2. trace: the persistent any-hit kernel over the slots, its ray count
+//      read from the device word the compaction filled (no host round trip);
+//   3. pack: a warp per tile word reads its 32 pixels' results through their
+//      slots and stores the ballot.
+// The words equal the shader's: every ray is traced with the plain kernel's
+// arithmetic, and a pixel without a ray contributes a zero bit.
 #include <algorithm>
 
 #include "engine.h"
-#include "traverse.cuh"
 
 namespace igxrt {
 
-struct ShadowArgs {
-    const float4* nodes;
-    const float4* prims;
-    uint32_t node_count;
-    const igxrt_ray* rays;
-    const uint32_t* object;
-    uint32_t width, height;
-    uint32_t tiles_x, tiles_y;
-    uint32_t words;
-    uint32_t* mask;
-    uint32_t* status;
-    uint32_t sh_depth;
-};
+namespace {
 
-template <int LAYOUT>
-__global__ void __launch_bounds__(256) shadow_mask_kernel(ShadowArgs a) {
-    extern __shared__ uint32_t smem[];
-    TraversalStack st;
-    st.sh = reinterpret_cast<uint2*>(smem) + threadIdx.x;
-    st.stride = blockDim.x;
-    st.sh_depth = a.sh_depth;
-    st.sp = 0;
+constexpr uint32_t kNoSlot = 0xffffffffu;
+
+__global__ void shadow_compact_kernel(const igxrt_ray* __restrict__ rays, const uint32_t* __restrict__ object,
+                                      uint32_t pixels, uint32_t nrays, igxrt_ray* __restrict__ crays,
+                                      uint32_t* __restrict__ cprev, uint32_t* __restrict__ slot_of,
+                                      uint32_t* __restrict__ count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t per_sample = a.tiles_x * a.tiles_y;
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < a.words; w += warps) {
-        const uint32_t s = w / per_sample, rem = w - s * per_sample;
-        const uint32_t ty = rem / a.tiles_x, tx = rem - ty * a.tiles_x;
-        const uint32_t x = tx * 16u + (lane & 15u), y = ty * 2u + (lane >> 4);
-        bool occ = false;
-        if (x < a.width && y < a.height) {
-            const uint32_t obj = __ldg(a.object + (size_t)y * a.width + x);
-            if (obj != IGXRT_NO_RAY_HIT) {
-                const uint32_t i = (uint32_t)(((size_t)s * a.height + y) * a.width + x);
-                const RayState r = load_ray(a.rays, i, obj);
-                BestHit best;
-                bool overflow = false;
-                occ = trace_single<LAYOUT, true>(a.nodes, a.prims, a.node_count, r, best, st, overflow);
-                if (overflow)
-                    atomicOr(a.status, kStatusStackOverflow);
-            }
-        }
-        const uint32_t bits = __ballot_sync(0xffffffffu, occ);
-        if (lane == 0)
-            __stcs(a.mask + w, bits);
+    uint32_t obj = IGXRT_NO_RAY_HIT;
+    if (i < nrays)
+        obj = __ldg(object + i % pixels);
+    const bool traced = obj != IGXRT_NO_RAY_HIT;
+    const uint32_t want = __ballot_sync(0xffffffffu, traced);
+    uint32_t base = 0;
+    if (lane == 0 && want)
+        base = atomicAdd(count, (uint32_t)__popc(want));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (i >= nrays)
+        return;
+    if (!traced) {
+        slot_of[i] = kNoSlot;
+        return;
     }
+    const uint32_t slot = base + __popc(want & ((1u << lane) - 1u));
+    const float4* src = reinterpret_cast<const float4*>(rays) + 2 * (size_t)i;
+    float4* dst = reinterpret_cast<float4*>(crays) + 2 * (size_t)slot;
+    dst[0] = __ldg(src);
+    dst[1] = __ldg(src + 1);
+    cprev[slot] = obj;
+    slot_of[i] = slot;
 }
+
+__global__ void shadow_pack_kernel(const uint32_t* __restrict__ slot_of, const uint32_t* __restrict__ occluded,
+                                   uint32_t width, uint32_t height, uint32_t tiles_x, uint32_t tiles_y,
+                                   uint32_t words, uint32_t* __restrict__ mask) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= words)
+        return;  // whole warps leave together (words are per warp)
+    const uint32_t per_sample = tiles_x * tiles_y;
+    const uint32_t s = w / per_sample, rem = w - s * per_sample;
+    const uint32_t ty = rem / tiles_x, tx = rem - ty * tiles_x;
+    const uint32_t x = tx * 16u + (lane & 15u), y = ty * 2u + (lane >> 4);
+    bool occ = false;
+    if (x < width && y < height) {
+        const uint32_t slot = __ldg(slot_of + ((size_t)s * height + y) * width + x);
+        occ = slot != kNoSlot && __ldg(occluded + slot) != 0u;
+    }
+    const uint32_t bits = __ballot_sync(0xffffffffu, occ);
+    if (lane == 0)
+        __stcs(mask + w, bits);
+}
+
+}  // namespace
 
 }  // namespace igxrt
 
@@ -99,65 +115,64 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
         return st;
     if (!scene->has_layout(p.layout))
         return fail(ctx, IGXRT_ERROR_UNSUPPORTED, format("the scene has no layout %u", p.layout));
+    const bool host = flags & IGXRT_TRACE_HOST_MEMORY;
+    if (!host && (!device_accessible(rays) || !device_accessible(object) || !device_accessible(mask)))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
     DeviceGuard guard(ctx->device);
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
     cudaStream_t stream = (cudaStream_t)stream_ptr;
-    const bool host = flags & IGXRT_TRACE_HOST_MEMORY;
+
+    // staging (host calls) and the pass's scratch, one growable buffer:
+    // [rays][object][mask] when staged, then [count][slot_of][cprev][occluded][crays]
+    const size_t rb = host ? round_up(nrays * sizeof(igxrt_ray), 256) : 0;
+    const size_t ob = host ? round_up(pixels * 4, 256) : 0;
+    const size_t mb = host ? round_up(words * 4, 256) : 0;
+    const size_t cb = 256, sb = round_up(nrays * 4, 256), pb = sb, occb = sb,
+                 crb = round_up(nrays * sizeof(igxrt_ray), 256);
+    st = grow_stage(ctx, rb + ob + mb + cb + sb + pb + occb + crb);
+    if (st != IGXRT_OK)
+        return st;
+    char* base = static_cast<char*>(ctx->d_stage);
     const igxrt_ray* d_rays = rays;
     const uint32_t* d_obj = object;
     uint32_t* d_mask = mask;
+    cudaError_t e = cudaSuccess;
     if (host) {
-        const size_t rb = (nrays * sizeof(igxrt_ray) + 255) / 256 * 256;
-        const size_t ob = (pixels * 4 + 255) / 256 * 256;
-        st = grow_stage(ctx, rb + ob + words * 4);
-        if (st != IGXRT_OK)
-            return st;
-        char* base = static_cast<char*>(ctx->d_stage);
         d_rays = reinterpret_cast<const igxrt_ray*>(base);
         d_obj = reinterpret_cast<const uint32_t*>(base + rb);
         d_mask = reinterpret_cast<uint32_t*>(base + rb + ob);
-        cudaError_t e = cudaMemcpyAsync(base, rays, nrays * sizeof(igxrt_ray), cudaMemcpyHostToDevice, stream);
+        e = cudaMemcpyAsync(base, rays, nrays * sizeof(igxrt_ray), cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(base + rb, object, pixels * 4, cudaMemcpyHostToDevice, stream);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "shadow upload");
-    } else if (!device_accessible(rays) || !device_accessible(object) || !device_accessible(mask)) {
-        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
-                    "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
     }
-    ShadowArgs a;
-    a.nodes = reinterpret_cast<const float4*>(scene->nodes[p.layout]);
-    a.prims = reinterpret_cast<const float4*>(scene->prims);
-    a.node_count = scene->node_count[p.layout];
-    a.rays = d_rays;
-    a.object = d_obj;
-    a.width = width;
-    a.height = height;
-    a.tiles_x = (uint32_t)tiles_x;
-    a.tiles_y = (uint32_t)tiles_y;
-    a.words = (uint32_t)words;
-    a.mask = d_mask;
-    a.status = status_word(ctx);
-    a.sh_depth = p.stack_depth;
-    auto fn = p.layout == IGXRT_LAYOUT_BVH8   ? shadow_mask_kernel<IGXRT_LAYOUT_BVH8>
-              : p.layout == IGXRT_LAYOUT_BVH4 ? shadow_mask_kernel<IGXRT_LAYOUT_BVH4>
-                                              : shadow_mask_kernel<IGXRT_LAYOUT_BVH2>;
-    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
-    int per_sm = 0;
-    cudaError_t e = allow_smem((const void*)fn, smem);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
-    if (e != cudaSuccess || per_sm < 1)
-        return e != cudaSuccess ? cuda_fail(ctx, e, "occupancy query")
-                                : fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "no resident CTA");
-    const uint64_t warps_per_block = p.block_size / 32;
-    const uint32_t grid = (uint32_t)std::max<uint64_t>(
-        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, (words + warps_per_block - 1) / warps_per_block));
-    fn<<<grid, p.block_size, smem, stream>>>(a);
+    char* scratch = base + rb + ob + mb;
+    uint32_t* d_count = reinterpret_cast<uint32_t*>(scratch);
+    uint32_t* d_slot = reinterpret_cast<uint32_t*>(scratch + cb);
+    uint32_t* d_prev = reinterpret_cast<uint32_t*>(scratch + cb + sb);
+    uint32_t* d_occ = reinterpret_cast<uint32_t*>(scratch + cb + sb + pb);
+    igxrt_ray* d_crays = reinterpret_cast<igxrt_ray*>(scratch + cb + sb + pb + occb);
+
+    e = cudaMemsetAsync(d_count, 0, 4, stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "shadow count reset");
+    shadow_compact_kernel<<<(uint32_t)((nrays + 255) / 256), 256, 0, stream>>>(
+        d_rays, d_obj, (uint32_t)pixels, (uint32_t)nrays, d_crays, d_prev, d_slot, d_count);
     e = cudaGetLastError();
     if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "shadow kernel launch");
+        return cuda_fail(ctx, e, "shadow compaction");
+    TraceRequest req{scene, d_crays, d_prev, (uint32_t)nrays, 1, nullptr, d_occ, nullptr, nullptr};
+    req.count_dev = d_count;
+    if ((st = launch_trace(ctx, req, p, stream)) != IGXRT_OK)
+        return st;
+    shadow_pack_kernel<<<(uint32_t)((words * 32 + 255) / 256), 256, 0, stream>>>(
+        d_slot, d_occ, width, height, (uint32_t)tiles_x, (uint32_t)tiles_y, (uint32_t)words, d_mask);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "shadow packing");
     if (host) {
         e = cudaMemcpyAsync(mask, d_mask, words * 4, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess)

@@ -28,6 +28,7 @@ struct KernelArgs {
     const igxrt_ray* rays;
     const uint32_t* prev;
     uint32_t count;
+    const uint32_t* count_dev;  // non-null: the ray count is this device word (at most `count`)
     igxrt_hit* hits;
     uint32_t* occluded;
     uint32_t* node_fetches;
@@ -86,6 +87,7 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
     bool alive = false, occluded_at_start = false;
     uint32_t ray = 0, nf = 0, pf = 0;
     int32_t next = kRefDone;
+    const uint32_t count = a.count_dev ? min(*a.count_dev, a.count) : a.count;
     RayState r;
     BestHit best;
     for (;;) {
@@ -100,12 +102,12 @@ __global__ void __launch_bounds__(256) trace_kernel(KernelArgs a) {
                     if (lane == 0)
                         b = atomicAdd(a.queue, a.packet);
                     b = __shfl_sync(0xffffffffu, b, 0);
-                    if (b >= a.count) {
+                    if (b >= count) {
                         queue_done = true;
                         break;
                     }
                     pk_base = b;
-                    pk_end = min(b + a.packet, a.count);
+                    pk_end = min(b + a.packet, count);
                 }
                 const uint32_t take = min(nidle - given, pk_end - pk_base);
                 if (!alive && rank >= given && rank < given + take) {
@@ -223,6 +225,7 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     a.rays = req.rays;
     a.prev = req.prev;
     a.count = req.count;
+    a.count_dev = req.count_dev;
     a.hits = req.hits;
     a.occluded = req.occluded;
     a.node_fetches = req.node_fetches;
@@ -274,6 +277,7 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
     a.rays = req.rays;
     a.prev = req.prev;
     a.count = req.count;
+    a.count_dev = req.count_dev;
     a.hits = req.hits;
     a.occluded = req.occluded;
     a.node_fetches = req.node_fetches;

@@ -954,7 +954,7 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,
                      dict(cfg, workload="shadowmask_sphere_1m_1080p_1_sample", rays_per_step=n,
                           light=list(scenes.SPHERE_LIGHT)),
-                     roofline=_roofline(b, ms, f"shadow_mask_kernel<{LAYOUT_NAMES[layout]}>"),
+                     roofline=_roofline(b, ms, f"shadow pass: compact + trace_kernel<{LAYOUT_NAMES[layout]},any> + pack"),
                      e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                           "h2d_bytes_per_step": 36 * w * h, "d2h_bytes_per_step": 4 * words,
                           "ms_per_step": round(e2e_ms, 3)},

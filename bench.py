@@ -28,8 +28,10 @@ value: Mrays/s over all rays of a step, inputs resident in device memory,
 CUDA-event time per step (L2 flushed between steps), plain kernels with the
 launch shape the engine's autotuner picks for the step.  batched: the same
 step as one graph-captured persistent launch.  e2e: the same rays through the
-C ABI with pinned host buffers (uploads and downloads inside the timed
-region).  --impl reference times the CPU transcription of the reference's
+C ABI with pinned host buffers, all host-device traffic inside the timed
+region: the kernels read the rays and write the results in place over
+NVLink-C2C (the default route), and beside it the staged route (copy up,
+trace, copy down).  --impl reference times the CPU transcription of the reference's
 traversal (the oracle's BVH traversal over the same BVH) on all host cores.
 """
 from __future__ import annotations
@@ -482,16 +484,27 @@ def run_engine(args, rank: int, world: int, local_rank: int):
             else:
                 ctx.trace_any(scene, hr, hp, out=ho)
 
-    for _ in range(args.warmup):
-        e2e_step()
-    e2e_times = []
-    for _ in range(args.steps):
-        flush.fill_(0.0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_ms = max_over_ranks(1000 * statistics.mean(e2e_times), dev)
+    def e2e_ms_per_step():
+        for _ in range(args.warmup):
+            e2e_step()
+        times = []
+        for _ in range(args.steps):
+            flush.fill_(0.0)  # no ray or result of the last step stays in L2
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_step()
+            times.append(time.perf_counter() - t0)
+        spread.append((round(1000 * min(times), 3), round(1000 * max(times), 3)))
+        return max_over_ranks(1000 * statistics.mean(times), dev)
+
+    spread = []  # (fastest, slowest) step of each route, ms
+    # default route: the kernels read the pinned rays and write the results
+    # in place over NVLink-C2C; then the same calls staged through device
+    # buffers (IGXRT_TRACE_STAGED: copy up, trace, copy down)
+    e2e_ms = e2e_ms_per_step()
+    ctx.stage_host_arrays = True
+    staged_ms = e2e_ms_per_step()
+    ctx.stage_host_arrays = False
     e2e_value = world * total_rays / (e2e_ms / 1e3) / 1e6
 
     if rank != 0:
@@ -510,7 +523,12 @@ def run_engine(args, rank: int, world: int, local_rank: int):
                               "unit": "GB/s", "frac": round(step_bytes / (step_ms / 1e3) / 1e9 / peaks["hbm_gbs"], 4)},
             "batches": per_batch,
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3)},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3),
+                    "ms_min_max": spread[0],
+                    "route": "pinned host arrays read and written in place by the kernels (NVLink-C2C)",
+                    "staged": {"value": round(world * total_rays / (staged_ms / 1e3) / 1e6, 3),
+                               "ms_per_step": round(staged_ms, 3), "ms_min_max": spread[1],
+                               "route": "IGXRT_TRACE_STAGED: copy up, trace, copy down"}},
             "gpu_launches": args.steps * nb,
             "clocks": clk,
             "wall_s_timed_region": round(wall, 3)}
@@ -611,11 +629,18 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
         bytes_total += algorithmic_bytes(nf, pf, 0, False, layout)
     achieved = bytes_total / (bat_ms / 1e3) / 1e9
 
-    # e2e: pinned host rays up, one batched launch, hits down
+    # e2e from pinned host memory: a batch whose items are the pinned arrays
+    # (the kernel reads the rays and writes the hits in place over
+    # NVLink-C2C); then the copy route: rays up, the device batch, hits down
     pinned = [torch.from_numpy(r.view(np.float32).reshape(-1, 8).copy()).pin_memory() for r in host_rays]
     hits_host = [torch.empty((len(r), 4), dtype=torch.float32).pin_memory() for r in host_rays]
+    batch_h = ctx.create_batch([(it[0], hr, None, hh, 0) for it, hr, hh in zip(items, pinned, hits_host)],
+                               params=tuned)
 
     def e2e():
+        batch_h.launch()
+
+    def copied():
         for (scene, d_rays, _, out, _), hr in zip(items, pinned):
             d_rays.copy_(hr, non_blocking=True)
         batch.launch()
@@ -623,6 +648,10 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
             hh.copy_(out, non_blocking=True)
 
     e2e_ms = statistics.mean(timed(e2e, args.steps))
+    same_h = all(torch.equal(hh.view(torch.int32), out.cpu().view(torch.int32))
+                 for (_, _, _, out, _), hh in zip(items, hits_host))
+    copied_ms = statistics.mean(timed(copied, args.steps))
+    batch_h.close()
     if rank != 0:
         return
     value = world * total_rays / (bat_ms / 1e3) / 1e6
@@ -650,7 +679,12 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
                          "peak_source": peaks["source"]},
             "e2e": {"value": round(world * total_rays / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                     "h2d_bytes_per_step": total_rays * RAY_BYTES,
-                    "d2h_bytes_per_step": total_rays * HIT_BYTES, "ms_per_step": round(e2e_ms, 3)},
+                    "d2h_bytes_per_step": total_rays * HIT_BYTES, "ms_per_step": round(e2e_ms, 3),
+                    "route": "batch items in pinned host memory, read and written in place by the kernel",
+                    "results_equal_device_batch": bool(same_h),
+                    "copied": {"value": round(world * total_rays / (copied_ms / 1e3) / 1e6, 3),
+                               "ms_per_step": round(copied_ms, 3),
+                               "route": "rays copied up, device batch, hits copied down"}},
             "gpu_launches": args.steps,
             "clocks": clk}
     print(json.dumps(line), flush=True)
@@ -889,8 +923,8 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         # the hit triangle's normals (48 B); no ray is read
         b = int(16 * len(rays) + (16 + 48) * int(hit.sum()) + NODE_BYTES[layout] * int(nf.sum(dtype=np.int64))
                 + PRIM_BYTES * int(pf.sum(dtype=np.int64)))
-        hdo = np.empty((h, w, 4), np.float32)
-        huv = np.empty((h, w, 4), np.float32)
+        hdo = torch.empty((h, w, 4), dtype=torch.float32).pin_memory().numpy()
+        huv = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory().numpy()
         ctx.trace_gbuffer(scene, cam, hdo, huv)
         e2e = []
         for _ in range(args.steps):
@@ -943,12 +977,16 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         n = int(hit.sum())
         b = int(32 * n + 4 * w * h + 4 * words + NODE_BYTES[layout] * int(nf.sum(dtype=np.int64))
                 + PRIM_BYTES * int(pf.sum(dtype=np.int64)))
-        hmask = np.empty(words, np.uint32)
-        ctx.trace_shadow_mask(scene, pix_rays, obj, w, h, 1, out=hmask)
+        # pinned host copies of the pass's inputs and mask
+        h_pix = torch.from_numpy(pix_rays.view(np.float32).reshape(-1, 8).copy()).pin_memory().numpy()
+        h_pix = h_pix.view(igx.RAY_DTYPE).reshape(-1)
+        h_obj = torch.from_numpy(obj.view(np.int32).copy()).pin_memory().numpy().view(np.uint32)
+        hmask = torch.empty(words, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+        ctx.trace_shadow_mask(scene, h_pix, h_obj, w, h, 1, out=hmask)
         e2e = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            ctx.trace_shadow_mask(scene, pix_rays, obj, w, h, 1, out=hmask)
+            ctx.trace_shadow_mask(scene, h_pix, h_obj, w, h, 1, out=hmask)
             e2e.append(time.perf_counter() - t0)
         e2e_ms = 1000 * statistics.mean(e2e)
         line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,

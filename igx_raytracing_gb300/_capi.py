@@ -22,6 +22,7 @@ LAYOUT_BVH4 = 1
 LAYOUT_BVH8 = 2
 LAYOUT_COUNT = 3
 TRACE_HOST_MEMORY = 1
+TRACE_STAGED = 2
 STATIC_SCRATCH_BYTES = 16 << 20
 STATIC_MAX_RAYS = 320000
 

@@ -22,7 +22,7 @@ from typing import Optional
 import numpy as np
 
 from . import _capi
-from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, RAY_DTYPE, TRACE_HOST_MEMORY,
+from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, RAY_DTYPE, TRACE_HOST_MEMORY, TRACE_STAGED,
                     TRIANGLE_DTYPE, BuildOptions, BvhInfo, IgxrtError, LaunchParams, check, lib)
 
 try:  # torch is only needed for device-memory calls
@@ -298,10 +298,17 @@ class Context:
         check(lib().igxrt_create(device, C.byref(h)), what=f"igxrt_create(device={device})")
         self._h = h
         self.device = device
+        # True: host arrays of trace, G-buffer, camera-ray and shadow-mask
+        # calls are staged through device buffers (IGXRT_TRACE_STAGED) even
+        # where the kernels could read and write them in place
+        self.stage_host_arrays = False
 
     @property
     def handle(self):
         return self._h
+
+    def _host_flags(self) -> int:
+        return TRACE_HOST_MEMORY | (TRACE_STAGED if self.stage_host_arrays else 0)
 
     def close(self) -> None:
         if self._h and self._h.value:
@@ -420,7 +427,7 @@ class Context:
         if n == 0:
             return out
         st = fn(self._h, scene.handle, r.ctypes.data, prev.ctypes.data if prev is not None else None,
-                n, out.ctypes.data, TRACE_HOST_MEMORY, self._stream(stream, False))
+                n, out.ctypes.data, self._host_flags(), self._stream(stream, False))
         check(st, self._h, "trace")
         return out
 
@@ -451,7 +458,7 @@ class Context:
             out = np.zeros(words, dtype=np.uint32)
         if words:
             check(fn(self._h, scene.handle, r.ctypes.data, obj.ctypes.data, width, height, samples,
-                     out.ctypes.data, TRACE_HOST_MEMORY, self._stream(stream, False)), self._h,
+                     out.ctypes.data, self._host_flags(), self._stream(stream, False)), self._h,
                   "shadow_mask")
         return out
 
@@ -471,7 +478,7 @@ class Context:
         if uv_normal is None:
             uv_normal = np.zeros((h, w, 4), dtype=np.float32)
         check(fn(self._h, scene.handle, cam.ctypes.data, dir_object.ctypes.data,
-                 uv_normal.ctypes.data, TRACE_HOST_MEMORY, self._stream(stream, False)), self._h,
+                 uv_normal.ctypes.data, self._host_flags(), self._stream(stream, False)), self._h,
               "gbuffer")
         return dir_object, uv_normal
 
@@ -486,7 +493,7 @@ class Context:
                   "camera_rays")
             return out
         rays = np.zeros(n, dtype=RAY_DTYPE)
-        check(fn(self._h, cam.ctypes.data, rays.ctypes.data if n else None, TRACE_HOST_MEMORY,
+        check(fn(self._h, cam.ctypes.data, rays.ctypes.data if n else None, self._host_flags(),
                  self._stream(stream, False)), self._h, "camera_rays")
         return rays
 
@@ -511,10 +518,13 @@ class Context:
     @staticmethod
     def batch_items(items) -> "C.Array":
         """items: iterables (scene, rays, prev_hit or None, out, mode) of CUDA
-        tensors; mode 0 = closest (out: (n,4) float32), 1 = any (out: n int32)."""
+        tensors or pinned CPU tensors (which the kernel reads and writes in
+        place); mode 0 = closest (out: (n,4) float32), 1 = any (out: n int32)."""
         arr = (_capi.BatchItem * max(1, len(items)))()
+        addressable = lambda t: _is_cuda_tensor(t) or (torch is not None and isinstance(t, torch.Tensor)
+                                                      and t.is_pinned())
         for i, (scene, rays, prev, out, mode) in enumerate(items):
-            assert _is_cuda_tensor(rays) and _is_cuda_tensor(out)
+            assert addressable(rays) and addressable(out) and (prev is None or addressable(prev))
             arr[i].scene = scene.handle.value
             arr[i].rays = rays.data_ptr()
             arr[i].prev_hit = prev.data_ptr() if prev is not None else None

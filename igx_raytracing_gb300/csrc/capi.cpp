@@ -149,6 +149,29 @@ bool igxrt::device_accessible(const void* p) {
            (attr.type == cudaMemoryTypeHost && attr.devicePointer != nullptr);
 }
 
+bool igxrt::host_direct(const igxrt_context* ctx, const void* p) {
+    if (!p)
+        return true;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged)
+        return true;
+    if (attr.type == cudaMemoryTypeHost)
+        return attr.devicePointer == p;  // pinned and mapped at the host address
+    return ctx->pageable_access;        // pageable memory
+}
+
+igxrt_status igxrt::check_trace_flags(igxrt_context* ctx, uint32_t flags) {
+    if (flags & ~(IGXRT_TRACE_HOST_MEMORY | IGXRT_TRACE_STAGED))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    if ((flags & IGXRT_TRACE_STAGED) && !(flags & IGXRT_TRACE_HOST_MEMORY))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "IGXRT_TRACE_STAGED needs IGXRT_TRACE_HOST_MEMORY");
+    return IGXRT_OK;
+}
+
 igxrt_status igxrt::check_scene(igxrt_context* ctx, const igxrt_scene* scene) {
     if (!scene)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "scene is NULL");
@@ -212,8 +235,8 @@ igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const ig
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "more than 2^31-1 rays in one call");
     if (!rays || !out)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "rays and output must be non-NULL");
-    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
-        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    if ((st = check_trace_flags(ctx, flags)) != IGXRT_OK)
+        return st;
     if (!aligned(rays, 16) || (mode == 0 && !aligned(out, 16)) || !aligned(out, 4) ||
         !aligned(prev, 4) || !aligned(nf, 4) || !aligned(pf, 4))
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
@@ -241,7 +264,23 @@ igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const ig
         return launch_trace(ctx, req, p, stream);
     }
 
-    // Host arrays: stage through the context's device buffer.
+    // Host arrays the kernel can address (pinned, or pageable on a device
+    // that reads it through the host's page tables): the kernel loads each
+    // ray once from host memory and stores each result once into it, over
+    // the chip-to-chip link, with no staging copies.
+    if (!(flags & IGXRT_TRACE_STAGED) && host_direct(ctx, rays) && host_direct(ctx, prev) &&
+        host_direct(ctx, out) && host_direct(ctx, nf) && host_direct(ctx, pf)) {
+        TraceRequest req{scene, rays, prev, count, mode, mode == 0 ? (igxrt_hit*)out : nullptr,
+                         mode == 1 ? (uint32_t*)out : nullptr, nf, pf};
+        if ((st = launch_trace(ctx, req, p, stream)) != IGXRT_OK)
+            return st;
+        const cudaError_t e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "trace");
+        return read_status(ctx);
+    }
+
+    // Other host arrays: stage through the context's device buffer.
     const size_t rb = round_up((size_t)count * sizeof(igxrt_ray), 256);
     const size_t pb = prev ? round_up((size_t)count * 4, 256) : 0;
     const size_t ob = round_up((size_t)count * out_elem, 256);
@@ -263,8 +302,7 @@ igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const ig
         return cuda_fail(ctx, e, "ray upload");
     TraceRequest req{scene, d_rays, d_prev, count, mode, mode == 0 ? (igxrt_hit*)d_out : nullptr,
                      mode == 1 ? (uint32_t*)d_out : nullptr, d_nf, d_pf};
-    st = launch_trace(ctx, req, p, stream);
-    if (st != IGXRT_OK)
+    if ((st = launch_trace(ctx, req, p, stream)) != IGXRT_OK)
         return st;
     e = cudaMemcpyAsync(out, d_out, (size_t)count * out_elem, cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess && nf) {
@@ -331,6 +369,12 @@ igxrt_status igxrt_create(int device, igxrt_context** out) {
         delete ctx;
         return IGXRT_ERROR_CUDA;
     }
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    ctx->pageable_access = pageable != 0;
     igxrt_launch_params defaults{};
     resolve_params(ctx, defaults, ctx->params);
     *out = ctx;

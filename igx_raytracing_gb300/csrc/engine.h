@@ -28,9 +28,13 @@ struct igxrt_context {
     uint32_t* d_words = nullptr;
     uint32_t next_slot = 0;
     igxrt_launch_params params{};
-    // Staging for IGXRT_TRACE_HOST_MEMORY traces (grown on demand).
+    // Staging for IGXRT_TRACE_HOST_MEMORY calls on host memory the kernels
+    // cannot address (grown on demand).
     void* d_stage = nullptr;
     size_t stage_bytes = 0;
+    // The device loads and stores pageable host memory through the host's
+    // page tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables).
+    bool pageable_access = false;
 };
 
 struct igxrt_scene {
@@ -156,6 +160,16 @@ igxrt_status read_status(igxrt_context* ctx);
 // True when a kernel may dereference p: device, managed or mapped pinned
 // memory (NULL counts as accessible).  Pageable host memory is not.
 bool device_accessible(const void* p);
+
+// True when the context's kernels may load and store p in place for a
+// host-memory call: device or managed memory, pinned host memory mapped at
+// the same address, or any host memory when the device reads pageable memory
+// through the host's page tables (Grace over NVLink-C2C).  NULL counts.
+bool host_direct(const igxrt_context* ctx, const void* p);
+
+// Flags of a trace-like call: IGXRT_TRACE_HOST_MEMORY, and
+// IGXRT_TRACE_STAGED only together with it.
+igxrt_status check_trace_flags(igxrt_context* ctx, uint32_t flags);
 
 // Makes ctx->device current for the lifetime of the guard.
 class DeviceGuard {

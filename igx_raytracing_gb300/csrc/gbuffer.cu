@@ -169,8 +169,8 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "image too large");
     if (((uintptr_t)dir_object % 16) || ((uintptr_t)uv_normal % 16))
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "images must be 16-byte aligned");
-    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
-        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    if ((st = check_trace_flags(ctx, flags)) != IGXRT_OK)
+        return st;
     igxrt_launch_params p;
     st = resolve_params(ctx, ctx->params, p);
     if (st != IGXRT_OK)
@@ -185,7 +185,11 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     float4* d_do = reinterpret_cast<float4*>(dir_object);
     float4* d_uv = reinterpret_cast<float4*>(uv_normal);
     const size_t ib = pixels * sizeof(float4);
-    if (host) {
+    // host images the kernel can address are written in place (a miss leaves
+    // the caller's uv_normal as it is); others are staged
+    const bool staged = host && ((flags & IGXRT_TRACE_STAGED) || !host_direct(ctx, dir_object) ||
+                                 !host_direct(ctx, uv_normal));
+    if (staged) {
         st = grow_stage(ctx, 2 * ((ib + 255) / 256 * 256));
         if (st != IGXRT_OK)
             return st;
@@ -195,7 +199,7 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
         const cudaError_t e = cudaMemcpyAsync(d_uv, uv_normal, ib, cudaMemcpyHostToDevice, stream);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "g-buffer upload");
-    } else if (!device_accessible(dir_object) || !device_accessible(uv_normal)) {
+    } else if (!host && (!device_accessible(dir_object) || !device_accessible(uv_normal))) {
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                     "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
     }
@@ -231,17 +235,18 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "g-buffer kernel launch");
-    if (host) {
+    if (!host)
+        return IGXRT_OK;
+    if (staged) {
         e = cudaMemcpyAsync(dir_object, d_do, ib, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(uv_normal, d_uv, ib, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess)
-            e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "g-buffer download");
-        return read_status(ctx);
     }
-    return IGXRT_OK;
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "g-buffer pass");
+    return read_status(ctx);
 }
 
 extern "C" igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera* cam, igxrt_ray* rays,
@@ -250,8 +255,8 @@ extern "C" igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera
         return IGXRT_ERROR_INVALID_ARGUMENT;
     if (!cam || !rays)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "camera and rays must be non-NULL");
-    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
-        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    if (const igxrt_status fst = check_trace_flags(ctx, flags))
+        return fst;
     const uint64_t pixels = (uint64_t)cam->width * cam->height;
     if (!pixels)
         return IGXRT_OK;
@@ -269,7 +274,9 @@ extern "C" igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera
     cudaStream_t stream = (cudaStream_t)stream_ptr;
     const size_t bytes = pixels * sizeof(igxrt_ray);
     float4* d_rays = reinterpret_cast<float4*>(rays);
-    if (host) {
+    // host rays the kernel can address are written in place, others staged
+    const bool staged = host && ((flags & IGXRT_TRACE_STAGED) || !host_direct(ctx, rays));
+    if (staged) {
         igxrt_status st = grow_stage(ctx, bytes);
         if (st != IGXRT_OK)
             return st;
@@ -278,11 +285,10 @@ extern "C" igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera
     camera_rays_kernel<<<(uint32_t)((pixels + 255) / 256), 256, 0, stream>>>(
         *cam, 1.0f / (float)cam->width, 1.0f / (float)cam->height, d_rays);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && host) {
+    if (e == cudaSuccess && staged)
         e = cudaMemcpyAsync(rays, d_rays, bytes, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess)
-            e = cudaStreamSynchronize(stream);
-    }
+    if (e == cudaSuccess && host)
+        e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "camera rays");
     return IGXRT_OK;

@@ -107,8 +107,8 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "rays, object and mask must be non-NULL");
     if (((uintptr_t)rays % 16) || ((uintptr_t)object % 4) || ((uintptr_t)mask % 4))
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "rays 16-byte aligned, object/mask 4-byte aligned");
-    if (flags & ~IGXRT_TRACE_HOST_MEMORY)
-        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
+    if ((st = check_trace_flags(ctx, flags)) != IGXRT_OK)
+        return st;
     igxrt_launch_params p;
     st = resolve_params(ctx, ctx->params, p);
     if (st != IGXRT_OK)
@@ -123,12 +123,17 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
     cudaStream_t stream = (cudaStream_t)stream_ptr;
+    // host arrays the kernels can address are read and written in place
+    // (the compaction gathers the traced rays into device memory); others
+    // are staged
+    const bool staged = host && ((flags & IGXRT_TRACE_STAGED) || !host_direct(ctx, rays) ||
+                                 !host_direct(ctx, object) || !host_direct(ctx, mask));
 
-    // staging (host calls) and the pass's scratch, one growable buffer:
+    // staging and the pass's scratch, one growable buffer:
     // [rays][object][mask] when staged, then [count][slot_of][cprev][occluded][crays]
-    const size_t rb = host ? round_up(nrays * sizeof(igxrt_ray), 256) : 0;
-    const size_t ob = host ? round_up(pixels * 4, 256) : 0;
-    const size_t mb = host ? round_up(words * 4, 256) : 0;
+    const size_t rb = staged ? round_up(nrays * sizeof(igxrt_ray), 256) : 0;
+    const size_t ob = staged ? round_up(pixels * 4, 256) : 0;
+    const size_t mb = staged ? round_up(words * 4, 256) : 0;
     const size_t cb = 256, sb = round_up(nrays * 4, 256), pb = sb, occb = sb,
                  crb = round_up(nrays * sizeof(igxrt_ray), 256);
     st = grow_stage(ctx, rb + ob + mb + cb + sb + pb + occb + crb);
@@ -139,7 +144,7 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
     const uint32_t* d_obj = object;
     uint32_t* d_mask = mask;
     cudaError_t e = cudaSuccess;
-    if (host) {
+    if (staged) {
         d_rays = reinterpret_cast<const igxrt_ray*>(base);
         d_obj = reinterpret_cast<const uint32_t*>(base + rb);
         d_mask = reinterpret_cast<uint32_t*>(base + rb + ob);
@@ -156,13 +161,11 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
     uint32_t* d_occ = reinterpret_cast<uint32_t*>(scratch + cb + sb + pb);
     igxrt_ray* d_crays = reinterpret_cast<igxrt_ray*>(scratch + cb + sb + pb + occb);
 
-    e = cudaMemsetAsync(d_count, 0, 4, stream);
-    if (e != cudaSuccess)
+    if ((e = cudaMemsetAsync(d_count, 0, 4, stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "shadow count reset");
     shadow_compact_kernel<<<(uint32_t)((nrays + 255) / 256), 256, 0, stream>>>(
         d_rays, d_obj, (uint32_t)pixels, (uint32_t)nrays, d_crays, d_prev, d_slot, d_count);
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
+    if ((e = cudaGetLastError()) != cudaSuccess)
         return cuda_fail(ctx, e, "shadow compaction");
     TraceRequest req{scene, d_crays, d_prev, (uint32_t)nrays, 1, nullptr, d_occ, nullptr, nullptr};
     req.count_dev = d_count;
@@ -170,16 +173,15 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
         return st;
     shadow_pack_kernel<<<(uint32_t)((words * 32 + 255) / 256), 256, 0, stream>>>(
         d_slot, d_occ, width, height, (uint32_t)tiles_x, (uint32_t)tiles_y, (uint32_t)words, d_mask);
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
+    if ((e = cudaGetLastError()) != cudaSuccess)
         return cuda_fail(ctx, e, "shadow packing");
-    if (host) {
+    if (!host)
+        return IGXRT_OK;
+    if (staged)
         e = cudaMemcpyAsync(mask, d_mask, words * 4, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess)
-            e = cudaStreamSynchronize(stream);
-        if (e != cudaSuccess)
-            return cuda_fail(ctx, e, "shadow download");
-        return read_status(ctx);
-    }
-    return IGXRT_OK;
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "shadow download");
+    return read_status(ctx);
 }

@@ -335,9 +335,18 @@ igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info
 
 /* ---- Ray queries --------------------------------------------------------- */
 
-/* rays, prev_hit and the output are host pointers: the call stages them
- * through device buffers and returns once the results are in host memory. */
+/* rays, prev_hit and the output are host pointers; the call returns once the
+ * results are in host memory.  When the kernels can address every one of
+ * them (pinned memory, or any host memory on a device that reads pageable
+ * memory through the host's page tables, as a GB300 does over NVLink-C2C)
+ * the kernels load the rays and store the results in place, each once;
+ * otherwise the call stages them through device buffers.  Trace, fetch
+ * count, G-buffer, camera-ray and shadow-mask calls take the flag. */
 #define IGXRT_TRACE_HOST_MEMORY 1u
+/* With IGXRT_TRACE_HOST_MEMORY (trace, G-buffer, camera-ray and shadow-mask
+ * calls): stage the host arrays through device buffers even when the kernels
+ * could address them in place. */
+#define IGXRT_TRACE_STAGED 2u
 
 /* Launch shape of the traversal kernels. Zero fields take the defaults. */
 typedef struct igxrt_launch_params {
@@ -409,6 +418,8 @@ igxrt_status igxrt_trace_closest_static(igxrt_context* ctx, const igxrt_scene* s
 #define IGXRT_MODE_ANY 1u
 
 /* One ray batch of a batched launch.  All pointers are device memory. */
+/* A batch item's arrays are device memory, or pinned host memory that the
+ * kernel reads and writes in place. */
 typedef struct igxrt_batch_item {
     const igxrt_scene* scene;
     const igxrt_ray* rays;

@@ -107,3 +107,37 @@ def test_camera_rays_split_the_gbuffer_pass(ctx):
     expect[:, :3] = np.where(hit[:, None], d * hits["t"][:, None].astype(np.float32), d)
     expect[:, 3] = hits["prim"].view(np.float32)
     assert np.array_equal(bits(g_do.reshape(-1, 4)), bits(expect))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("memory", ["pageable", "pinned", "staged"])
+def test_gbuffer_host_routes_match_oracle(ctx, memory):
+    """Host images the kernel can address are written in place, so a miss
+    leaves the caller's uv_normal untouched without an upload; staged images
+    carry it through the device.  Both equal the oracle, on a ragged image
+    (the last tile row and column half outside it)."""
+    w, h = 613, 389
+    tris = normals_scene()
+    cam = scenes.camera_record(w, h, eye=(0.5, -1.2, 0.6), target=(0.5, 0.5, 0.45), jitter=(0.25, 0.75))
+    e_do, e_uv, flags = pyoracle.gbuffer(tris, cam, uv_fill=-3.0)
+    assert not flags.any()
+    scene = ctx.create_scene(tris)
+    if memory == "pinned":
+        import torch
+
+        g_do = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory().numpy()
+        g_uv = torch.full((h, w, 4), -3.0, dtype=torch.float32).pin_memory().numpy()
+    else:
+        g_do = np.zeros((h, w, 4), dtype=np.float32)
+        g_uv = np.full((h, w, 4), -3.0, dtype=np.float32)
+    ctx.stage_host_arrays = memory == "staged"
+    try:
+        ctx.trace_gbuffer(scene, cam, g_do, g_uv)
+        rays = ctx.camera_rays(cam)
+    finally:
+        ctx.stage_host_arrays = False
+    assert np.array_equal(bits(g_do), bits(e_do))
+    assert np.array_equal(bits(g_uv), bits(e_uv))
+    hit = g_do[..., 3].view(np.uint32) != 0xFFFFFFFF
+    assert hit.any() and (~hit).any()
+    assert rays.tobytes() == ctx.camera_rays(cam).tobytes()

@@ -89,3 +89,51 @@ def test_shadow_mask_device_memory(ctx):
     got = ctx.trace_shadow_mask(scene, d_rays, d_obj, w, h, s)
     torch.cuda.synchronize()
     assert np.array_equal(got.cpu().numpy().view(np.uint32), expect)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("memory", ["pageable", "pinned", "staged"])
+def test_shadow_mask_host_routes_match_device_pass(ctx, memory):
+    """Host arrays the kernels can address are read in place by the
+    compaction (which gathers the traced rays into device memory) and the
+    mask is stored in place; staged arrays go through device buffers.  The
+    words equal the device-memory pass, which the tests above pin to the
+    oracle; two samples make the object index wrap."""
+    import torch
+
+    w, h, s = 300, 200, 2
+    tris = scenes.heightfield(64, 32, scenes.seed_for(1, 77))
+    prim = scenes.pinhole_rays(w, h, eye=(0.5, -1.0, 0.5), target=(0.5, 0.5, 0.0))
+    scene = ctx.create_scene(tris)
+    hits = scene.trace_geometry(prim)
+    obj = hits["prim"].copy()
+    o = prim["org"] + hits["t"][:, None] * prim["dir"]
+    o[obj == NO_RAY_HIT] = 0.0
+    rays = np.zeros(w * h * s, dtype=RAY_DTYPE)
+    for k, light in enumerate(([0.2, 0.3, 1.5], [0.8, 0.6, 1.2])):
+        d = np.asarray(light, np.float32) - o
+        dist = np.linalg.norm(d, axis=1).astype(np.float32)
+        dist[dist == 0] = 1.0
+        sl = slice(k * w * h, (k + 1) * w * h)
+        rays["org"][sl] = o
+        rays["dir"][sl] = d / dist[:, None]
+        rays["tmax"][sl] = dist
+    words = ((w + 15) // 16) * ((h + 1) // 2) * s
+    if memory == "pinned":
+        h_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory().numpy()
+        h_rays = h_rays.view(RAY_DTYPE).reshape(-1)
+        h_obj = torch.from_numpy(obj.view(np.int32).copy()).pin_memory().numpy().view(np.uint32)
+        out = torch.zeros(words, dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    else:
+        h_rays, h_obj, out = rays, obj, np.zeros(words, dtype=np.uint32)
+    ctx.stage_host_arrays = memory == "staged"
+    try:
+        got = ctx.trace_shadow_mask(scene, h_rays, h_obj, w, h, s, out=out)
+    finally:
+        ctx.stage_host_arrays = False
+    d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    d_obj = torch.from_numpy(obj.view(np.int32).copy()).cuda()
+    expect = ctx.trace_shadow_mask(scene, d_rays, d_obj, w, h, s)
+    torch.cuda.synchronize()
+    assert np.array_equal(got, expect.cpu().numpy().view(np.uint32))
+    assert got.any() and (obj == NO_RAY_HIT).any()

@@ -173,3 +173,62 @@ def test_determinism_and_permutation_invariance(ctx):
     perm = np.random.default_rng(0).permutation(len(rays))
     c = scene.trace_geometry(rays[perm])
     assert a[perm].tobytes() == c.tobytes()
+
+
+def host_copy(a, memory):
+    """a as pageable numpy memory, or in pinned host memory."""
+    if memory != "pinned":
+        return a.copy()
+    import torch
+
+    raw = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
+    buf = torch.empty(raw.size, dtype=torch.uint8).pin_memory().numpy()
+    buf[:] = raw
+    return buf.view(a.dtype).reshape(a.shape)
+
+
+@pytest.mark.parametrize("memory", ["pageable", "pinned", "staged"])
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_host_array_routes_match_the_cpu_traversal(params, layout, memory):
+    """Host arrays the kernels can address (pinned, or pageable on a device
+    that reads host page tables) are read and written in place; with
+    IGXRT_TRACE_STAGED they go through device buffers.  Every route gives the
+    CPU traversal's hits, occlusion words and fetch counts."""
+    ctx = params
+    tris = scenes.random_triangles(20000, 93, mu=math.log(0.01))
+    rays = host_copy(scenes.incoherent_rays(300_000, 94), memory)
+    b = BVH.build(tris)
+    scene = ctx.create_scene(bvh=b)
+    nodes, prims = b.arrays(layout)
+    ctx.set_launch_params(layout=layout)
+    ctx.stage_host_arrays = memory == "staged"
+    try:
+        hits = host_copy(np.zeros(len(rays), dtype=HIT_DTYPE), memory)
+        ctx.trace_closest(scene, rays, out=hits)
+        expect, nf, pf = pyoracle.bvh_trace(layout, nodes, prims, rays, mode=0, counts=True)
+        assert hits.tobytes() == expect.tobytes()
+        gnf, gpf = ctx.count_fetches(scene, rays, mode=0, layout=layout)
+        assert np.array_equal(gnf, nf) and np.array_equal(gpf, pf)
+        sh = rays.copy()
+        sh["tmax"] = 0.2
+        sh = host_copy(sh, memory)
+        prev = host_copy(hits["prim"].copy(), memory)
+        occ = host_copy(np.zeros(len(rays), dtype=np.uint32), memory)
+        ctx.trace_any(scene, sh, prev, out=occ)
+        assert np.array_equal(occ, pyoracle.bvh_trace(layout, nodes, prims, sh, prev=prev, mode=1))
+        assert occ.any() and not occ.all()
+    finally:
+        ctx.stage_host_arrays = False
+
+
+def test_staged_flag_needs_the_host_flag(ctx, engine_lib):
+    import ctypes as C
+
+    tris = scenes.random_triangles(100, 95)
+    scene = ctx.create_scene(tris)
+    rays = scenes.incoherent_rays(64, 96)
+    out = np.zeros(64, dtype=HIT_DTYPE)
+    st = engine_lib.igxrt_trace_closest(ctx.handle, scene.handle, rays.ctypes.data, None, 64,
+                                        out.ctypes.data, 2, C.c_void_p(0))
+    assert st == 1
+    assert b"IGXRT_TRACE_STAGED" in engine_lib.igxrt_last_error(ctx.handle)

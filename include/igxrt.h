@@ -550,6 +550,9 @@ igxrt_status igxrt_server_destroy(igxrt_server* server);
  *           0; otherwise its rays exclude that object (prevHit).
  *   mask:   tiles_x*tiles_y*samples words, every one written (the shader's
  *           non-DEBUG build leaves all-empty tiles unwritten; here they are 0).
+ * The pass compacts the traced rays into the context's staging buffer, so two
+ * shadow passes (or a shadow pass and a host-memory call) of one context must
+ * not overlap on different streams.
  */
 igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_scene* scene,
                                      const igxrt_ray* rays, const uint32_t* object,

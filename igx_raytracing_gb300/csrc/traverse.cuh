@@ -165,6 +165,19 @@ struct TraversalStack {
             spill[sp - sh_depth] = e;
         ++sp;
     }
+    __device__ __forceinline__ uint2 at(uint32_t k) const { return k < sh_depth ? sh[k * stride] : spill[k - sh_depth]; }
+    __device__ __forceinline__ void set(uint32_t k, uint2 e) {
+        if (k < sh_depth)
+            sh[k * stride] = e;
+        else
+            spill[k - sh_depth] = e;
+    }
+    // Removes the g bottom entries; the rest move down g places.
+    __device__ void drop_bottom(uint32_t g) {
+        for (uint32_t k = g; k < sp; ++k)
+            set(k - g, at(k));
+        sp -= g;
+    }
     __device__ __forceinline__ int32_t pop_live(float tcull) {
         while (sp) {
             --sp;

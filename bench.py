@@ -161,20 +161,24 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, interval_ms: int = 20):
+        """interval_ms: 20 covers timed regions of a few ms; a long serving
+        run samples every 250 ms, since each nvidia-smi query briefly holds
+        driver locks that the serving thread's CUDA calls then wait on."""
         self.device = device
+        self.interval_ms = interval_ms
         self.proc = None
         self.path = os.path.join(REPO, "gpurun_out", f"clocks_dev{device}.csv")
 
     def start(self):
-        """Starts sampling every 20 ms and returns once the first sample is in,
-        so even a short timed region that follows is covered."""
+        """Starts sampling and returns once the first sample is in, so even a
+        short timed region that follows is covered."""
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.fh,
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)], stdout=self.fh,
                 stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -762,7 +766,7 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
                          max_batch_requests=max_batch_requests)
         ids = [srv.add_scene(s) for s in sc]
         tickets = [0] * n_req
-        clocks = ClockSampler(local_rank)
+        clocks = ClockSampler(local_rank, interval_ms=250)
         if with_clocks:
             clocks.start()
 

@@ -23,6 +23,7 @@ LAYOUT_BVH8 = 2
 LAYOUT_COUNT = 3
 TRACE_HOST_MEMORY = 1
 TRACE_STAGED = 2
+TRACE_INDEPENDENT = 4
 STATIC_SCRATCH_BYTES = 16 << 20
 STATIC_MAX_RAYS = 320000
 

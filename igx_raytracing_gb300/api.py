@@ -22,8 +22,9 @@ from typing import Optional
 import numpy as np
 
 from . import _capi
-from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, RAY_DTYPE, TRACE_HOST_MEMORY, TRACE_STAGED,
-                    TRIANGLE_DTYPE, BuildOptions, BvhInfo, IgxrtError, LaunchParams, check, lib)
+from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, RAY_DTYPE, TRACE_HOST_MEMORY,
+                    TRACE_INDEPENDENT, TRACE_STAGED, TRIANGLE_DTYPE, BuildOptions, BvhInfo, IgxrtError,
+                    LaunchParams, check, lib)
 
 try:  # torch is only needed for device-memory calls
     import torch
@@ -399,7 +400,7 @@ class Context:
             return C.c_void_p(torch.cuda.current_stream().cuda_stream)
         return C.c_void_p(0)
 
-    def _trace(self, scene: Scene, rays, prev_hit, mode: int, stream, out=None):
+    def _trace(self, scene: Scene, rays, prev_hit, mode: int, stream, out=None, independent=False):
         fn = lib().igxrt_trace_closest if mode == 0 else lib().igxrt_trace_any
         if _is_cuda_tensor(rays):
             assert rays.dtype == torch.float32 and rays.is_contiguous() and rays.shape[-1] == 8
@@ -411,8 +412,8 @@ class Context:
             if prev_hit is not None:
                 assert _is_cuda_tensor(prev_hit) and prev_hit.dtype == torch.int32
                 prev_ptr = prev_hit.data_ptr()
-            st = fn(self._h, scene.handle, rays.data_ptr(), prev_ptr, n, out.data_ptr(), 0,
-                    self._stream(stream, True))
+            st = fn(self._h, scene.handle, rays.data_ptr(), prev_ptr, n, out.data_ptr(),
+                    TRACE_INDEPENDENT if independent else 0, self._stream(stream, True))
             check(st, self._h, "trace")
             return out
         r = as_rays(rays)
@@ -431,11 +432,17 @@ class Context:
         check(st, self._h, "trace")
         return out
 
-    def trace_closest(self, scene: Scene, rays, prev_hit=None, stream=None, out=None):
-        return self._trace(scene, rays, prev_hit, 0, stream, out)
+    def trace_closest(self, scene: Scene, rays, prev_hit=None, stream=None, out=None,
+                      independent: bool = False):
+        """independent=True (CUDA tensors): IGXRT_TRACE_INDEPENDENT, this call
+        neither reads what the kernel queued before it on the stream writes
+        nor writes what that kernel touches, so it may start during that
+        kernel's last rays."""
+        return self._trace(scene, rays, prev_hit, 0, stream, out, independent)
 
-    def trace_any(self, scene: Scene, rays, prev_hit=None, stream=None, out=None):
-        return self._trace(scene, rays, prev_hit, 1, stream, out)
+    def trace_any(self, scene: Scene, rays, prev_hit=None, stream=None, out=None,
+                  independent: bool = False):
+        return self._trace(scene, rays, prev_hit, 1, stream, out, independent)
 
     def trace_shadow_mask(self, scene: Scene, rays, object_, width: int, height: int,
                           samples: int, stream=None, out=None):

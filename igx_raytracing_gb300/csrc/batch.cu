@@ -316,10 +316,15 @@ igxrt_status igxrt_trace_batch(igxrt_context* ctx, const igxrt_batch_item* items
                                     cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "batch table upload");
-    st = launch_batch(ctx, d_table, count, packets, rays, p, take_queue_slot(ctx), stream);
+    uint32_t* queue = take_queue_slot(ctx);
+    st = launch_batch(ctx, d_table, count, packets, rays, p, queue, stream);
     if (st != IGXRT_OK)
         return st;
-    e = cudaEventRecord(*done, stream);
+    // the ring's slots are zero between launches (trace launches skip the
+    // reset and rely on it)
+    e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), stream);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(*done, stream);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "batch slot event");
     return IGXRT_OK;

@@ -164,8 +164,8 @@ bool igxrt::host_direct(const igxrt_context* ctx, const void* p) {
     return ctx->pageable_access;        // pageable memory
 }
 
-igxrt_status igxrt::check_trace_flags(igxrt_context* ctx, uint32_t flags) {
-    if (flags & ~(IGXRT_TRACE_HOST_MEMORY | IGXRT_TRACE_STAGED))
+igxrt_status igxrt::check_trace_flags(igxrt_context* ctx, uint32_t flags, uint32_t extra) {
+    if (flags & ~(IGXRT_TRACE_HOST_MEMORY | IGXRT_TRACE_STAGED | extra))
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown flags 0x%x", flags));
     if ((flags & IGXRT_TRACE_STAGED) && !(flags & IGXRT_TRACE_HOST_MEMORY))
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "IGXRT_TRACE_STAGED needs IGXRT_TRACE_HOST_MEMORY");
@@ -235,7 +235,7 @@ igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const ig
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "more than 2^31-1 rays in one call");
     if (!rays || !out)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "rays and output must be non-NULL");
-    if ((st = check_trace_flags(ctx, flags)) != IGXRT_OK)
+    if ((st = check_trace_flags(ctx, flags, IGXRT_TRACE_INDEPENDENT)) != IGXRT_OK)
         return st;
     if (!aligned(rays, 16) || (mode == 0 && !aligned(out, 16)) || !aligned(out, 4) ||
         !aligned(prev, 4) || !aligned(nf, 4) || !aligned(pf, 4))
@@ -261,6 +261,7 @@ igxrt_status trace_common(igxrt_context* ctx, const igxrt_scene* scene, const ig
                         "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
         TraceRequest req{scene, rays, prev, count, mode, mode == 0 ? (igxrt_hit*)out : nullptr,
                          mode == 1 ? (uint32_t*)out : nullptr, nf, pf};
+        req.independent = (flags & IGXRT_TRACE_INDEPENDENT) != 0;
         return launch_trace(ctx, req, p, stream);
     }
 
@@ -361,8 +362,8 @@ igxrt_status igxrt_create(int device, igxrt_context** out) {
     if (cudaGetDeviceProperties(&prop, device) == cudaSuccess)
         ctx->device_name = prop.name;
     if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-        cudaMalloc(&ctx->d_words, (kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMemset(ctx->d_words, 0, (kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess) {
+        cudaMalloc(&ctx->d_words, (2 * kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemset(ctx->d_words, 0, (2 * kQueueSlots + 1) * sizeof(uint32_t)) != cudaSuccess) {
         cudaGetLastError();
         if (ctx->d_words)
             cudaFree(ctx->d_words);

@@ -24,7 +24,8 @@ struct igxrt_context {
     void* d_batch = nullptr;
     cudaEvent_t batch_events[igxrt::kBatchSlots] = {};
     uint32_t next_batch_slot = 0;
-    // Device words: kQueueSlots work-queue counters, then the error word.
+    // Device words: kQueueSlots work-queue counters, the error word, then one
+    // exit counter per queue slot (see launch_trace).
     uint32_t* d_words = nullptr;
     uint32_t next_slot = 0;
     igxrt_launch_params params{};
@@ -98,6 +99,9 @@ struct TraceRequest {
     // non-null: the number of rays is this device word (written by an earlier
     // kernel on the stream), at most `count`, which sizes the launch
     const uint32_t* count_dev = nullptr;
+    // IGXRT_TRACE_INDEPENDENT: the kernel need not wait for the kernel
+    // queued before it on the stream
+    bool independent = false;
 };
 
 // Records `msg` as the context's last error and returns `st`.
@@ -138,8 +142,10 @@ igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint3
                           uint32_t total_packets, uint64_t total_rays, const igxrt_launch_params& p,
                           uint32_t* queue, cudaStream_t stream);
 
-// Next work-queue counter of the context (a ring of kQueueSlots words).
+// Next work-queue counter of the context (a ring of kQueueSlots words); the
+// slot's exit counter is exit_word(slot).
 uint32_t* take_queue_slot(igxrt_context* ctx);
+inline uint32_t* exit_word(uint32_t* queue_slot) { return queue_slot + kQueueSlots + 1; }
 uint32_t* status_word(igxrt_context* ctx);
 
 // Opts a kernel into more than 48 KB of dynamic shared memory when `smem`
@@ -167,9 +173,9 @@ bool device_accessible(const void* p);
 // through the host's page tables (Grace over NVLink-C2C).  NULL counts.
 bool host_direct(const igxrt_context* ctx, const void* p);
 
-// Flags of a trace-like call: IGXRT_TRACE_HOST_MEMORY, and
-// IGXRT_TRACE_STAGED only together with it.
-igxrt_status check_trace_flags(igxrt_context* ctx, uint32_t flags);
+// Flags of a trace-like call: IGXRT_TRACE_HOST_MEMORY, IGXRT_TRACE_STAGED
+// only together with it, and the bits of `extra` the call also takes.
+igxrt_status check_trace_flags(igxrt_context* ctx, uint32_t flags, uint32_t extra = 0);
 
 // Makes ctx->device current for the lifetime of the guard.
 class DeviceGuard {

@@ -41,6 +41,10 @@ struct KernelArgs {
     const float4* planes;  // mixed scenes: planes outside the tree
     uint32_t plane_count;
     uint32_t plane_base;   // object id of the first plane
+    // non-null: the queue slot's exit counter; the last warp to leave zeroes
+    // it and the queue word, so the slot needs no reset before its next launch
+    uint32_t* exit_count;
+    uint32_t independent;  // IGXRT_TRACE_INDEPENDENT: no wait for the kernel before
 };
 
 template <bool ANY, bool COUNT, bool MIXED>
@@ -227,6 +231,11 @@ constexpr int trace_kernel_regs(int layout, bool any, bool mixed) {
 // when a ray starts, priority-coded best hit).
 template <int LAYOUT, bool ANY, bool COUNT, bool MIXED>
 __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(KernelArgs a) {
+    // Launched with programmatic stream serialization: unless the caller
+    // stated independence, wait until the kernel queued before this one has
+    // finished and its writes are visible (a no-op after any other work)
+    if (!a.independent)
+        asm volatile("griddepcontrol.wait;" ::: "memory");
     extern __shared__ uint32_t smem[];
     TraversalStack st;
     st.sh = reinterpret_cast<uint2*>(smem) + threadIdx.x;
@@ -264,6 +273,9 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
                     b = __shfl_sync(0xffffffffu, b, 0);
                     if (b >= count) {
                         queue_done = true;
+                        // every ray is claimed: the next kernel on the stream
+                        // may start on the SMs this launch's tail leaves idle
+                        asm volatile("griddepcontrol.launch_dependents;");
                         break;
                     }
                     pk_base = b;
@@ -321,6 +333,15 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
                     alive = false;
                 }
             }
+        }
+    }
+    if (a.exit_count && lane == 0) {
+        // every warp's queue claims come before its exit count
+        __threadfence();
+        const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+        if (atomicAdd(a.exit_count, 1u) == warps - 1u) {
+            *a.queue = 0u;
+            *a.exit_count = 0u;
         }
     }
 }
@@ -403,11 +424,22 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     a.planes = reinterpret_cast<const float4*>(s->planes);
     a.plane_count = s->plane_count;
     a.plane_base = s->plane_base;
-    e = cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), stream);
-    if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "queue reset");
-    fn<<<grid, p.block_size, smem, stream>>>(a);
-    e = cudaGetLastError();
+    // the slot's words are zero (zeroed at context creation, and by the last
+    // warp of the slot's previous launch), so no reset sits between this
+    // launch and the kernel before it
+    a.exit_count = exit_word(a.queue);
+    a.independent = req.independent ? 1u : 0u;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(p.block_size);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, fn, a);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "trace kernel launch");
     return IGXRT_OK;
@@ -449,6 +481,8 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
     a.prim_fetches = req.prim_fetches;
     a.queue = queue;
     a.status = status;
+    a.exit_count = nullptr;  // the caller resets its words
+    a.independent = 0u;
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;

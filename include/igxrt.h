@@ -347,6 +347,15 @@ igxrt_status igxrt_scene_get_info(const igxrt_scene* scene, igxrt_bvh_info* info
  * calls): stage the host arrays through device buffers even when the kernels
  * could address them in place. */
 #define IGXRT_TRACE_STAGED 2u
+/* igxrt_trace_closest / igxrt_trace_any on device memory: the caller states
+ * that this call reads nothing the kernel queued just before it on `stream`
+ * writes, and writes nothing that kernel reads or writes (e.g. shadow rays
+ * traced after bounce rays, both made from the same primary hits).  The
+ * traversal kernel may then start while that kernel drains its last rays
+ * (programmatic dependent launch).  Without the flag a trace kernel starts
+ * its work only after the kernel before it has finished and its writes are
+ * visible, as for any stream-ordered launch. */
+#define IGXRT_TRACE_INDEPENDENT 4u
 
 /* Launch shape of the traversal kernels. Zero fields take the defaults. */
 typedef struct igxrt_launch_params {

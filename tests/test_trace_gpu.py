@@ -232,3 +232,87 @@ def test_staged_flag_needs_the_host_flag(ctx, engine_lib):
                                         out.ctypes.data, 2, C.c_void_p(0))
     assert st == 1
     assert b"IGXRT_TRACE_STAGED" in engine_lib.igxrt_last_error(ctx.handle)
+
+
+def _quad_scene():
+    """Triangles 0 and 1: a 4x4 quad at z = 1; behind it, at z = 2, a grid of
+    small triangles.  Rays toward +z hit triangle 0 or 1 unless prev_hit
+    excludes it."""
+    back = scenes.heightfield(32, 32, scenes.seed_for(3, 1))
+    back["p0"][:, 2] = 2.0
+    back["p1"][:, 2] = 2.0
+    back["p2"][:, 2] = 2.0
+    quad = np.zeros(2, dtype=TRIANGLE_DTYPE)
+    quad["p0"] = [(-1.5, -1.5, 1.0), (2.5, 2.5, 1.0)]
+    quad["p1"] = [(2.5, -1.5, 1.0), (-1.5, 2.5, 1.0)]
+    quad["p2"] = [(-1.5, 2.5, 1.0), (2.5, -1.5, 1.0)]
+    return np.concatenate([quad, back])
+
+
+def _up_rays(n, seed):
+    rng = np.random.default_rng(seed)
+    rays = np.zeros(n, dtype=scenes.RAY_DTYPE)
+    rays["org"][:, :2] = rng.uniform(0.05, 0.95, (n, 2))
+    rays["dir"] = (0.0, 0.0, 1.0)
+    rays["tmax"] = np.float32(3.4028235e38)
+    return rays
+
+
+def test_a_launch_sees_the_writes_of_the_trace_before_it(ctx):
+    """Trace launches may start while the kernel before them drains; without
+    IGXRT_TRACE_INDEPENDENT the kernel waits for that kernel's writes before
+    reading its inputs.  Here the second trace's prev_hit is the first one's
+    output (0 or 1 per ray), which decides almost every closest hit."""
+    import torch
+
+    tris = _quad_scene()
+    scene = ctx.create_scene(tris)
+    n = 600_000
+    a_rays = _up_rays(n, 5)
+    a_rays["tmax"] = np.where(np.arange(n) % 3 == 0, 0.5, 1.5).astype(np.float32)  # occluded iff tmax > 1
+    b_rays = _up_rays(n, 6)
+    d_a = torch.from_numpy(a_rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    d_b = torch.from_numpy(b_rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    for rep in range(3):
+        occ = torch.full((n,), -1, dtype=torch.int32, device="cuda")  # stale: no exclusion
+        hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        ctx.trace_any(scene, d_a, out=occ)
+        ctx.trace_closest(scene, d_b, occ, out=hits)
+        torch.cuda.synchronize()
+        prev = occ.cpu().numpy().view(np.uint32)
+        assert set(np.unique(prev)) == {0, 1}
+        got = hits.cpu().numpy().view(HIT_DTYPE).reshape(-1)
+        expect = scene.trace_geometry(b_rays, prev)
+        assert got.tobytes() == expect.tobytes()
+        assert (got["prim"] >= 2).sum() > n // 3  # the exclusions mattered
+
+
+def test_independent_launches_and_queue_slot_reuse(ctx):
+    """IGXRT_TRACE_INDEPENDENT launches give the results of the same calls
+    made one at a time; 4,200 back-to-back launches wrap the context's ring of
+    4,096 queue slots, each left zeroed by its previous launch's last warp."""
+    import torch
+
+    tris = _quad_scene()
+    scene = ctx.create_scene(tris)
+    rays = _up_rays(4096, 7)
+    rays["tmax"] = np.where(np.arange(4096) % 2 == 0, 0.5, 1.5).astype(np.float32)
+    expect_hits = scene.trace_geometry(rays)
+    expect_occ = scene.trace_occlusion(rays)
+    d_r = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+    outs_h = [torch.empty((64, 4), dtype=torch.float32, device="cuda") for _ in range(64)]
+    outs_o = [torch.empty(64, dtype=torch.int32, device="cuda") for _ in range(64)]
+    for k in range(4200):
+        j = (k // 2) % 64  # every slice gets both queries, many times over
+        sl = slice(64 * j, 64 * (j + 1))
+        if k % 2 == 0:
+            ctx.trace_closest(scene, d_r[sl], out=outs_h[j], independent=True)
+        else:
+            ctx.trace_any(scene, d_r[sl], out=outs_o[j], independent=True)
+    torch.cuda.synchronize()
+    ctx.sync()
+    got_h = torch.cat(outs_h).cpu().numpy().view(HIT_DTYPE).reshape(-1)
+    got_o = torch.cat(outs_o).cpu().numpy().view(np.uint32)
+    assert got_h.tobytes() == expect_hits.tobytes()
+    assert np.array_equal(got_o, expect_occ)
+    assert expect_occ.any() and not expect_occ.all()

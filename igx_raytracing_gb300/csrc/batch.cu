@@ -9,13 +9,15 @@
 // finish rays of one scene while starting rays of the next, and the GPU stays
 // full across item boundaries instead of draining at the end of each launch.
 // Per ray the traversal is the plain kernel's (same visiting order, same
-// arithmetic), so results equal tracing each item alone.
+// arithmetic, and the same tail work sharing once the queue is drained), so
+// results equal tracing each item alone.
 #include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "engine.h"
+#include "share.cuh"
 #include "traverse.cuh"
 
 namespace igxrt {
@@ -31,6 +33,35 @@ struct BatchArgs {
     uint32_t packet;
     uint32_t sh_depth;
     uint32_t refill_lanes;
+};
+
+// A finished ray's record: occluded word (any hit) or hit (closest).
+__device__ __forceinline__ void write_result(void* out, uint32_t mode, uint32_t ray, const RayState& r,
+                                             const BestHit& best, bool occluded) {
+    if (mode) {
+        __stcs(static_cast<uint32_t*>(out) + ray, occluded ? 1u : 0u);
+    } else {
+        const bool hit = best.t < r.tmax_eff;
+        const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(best.prim))
+                             : make_float4(IGXRT_NO_HIT, 0.f, 0.f, __uint_as_float(IGXRT_NO_RAY_HIT));
+        __stcs(static_cast<float4*>(out) + ray, h);
+    }
+}
+
+// A lane's item (scene arrays, output, query mode), which a helper in the
+// tail copies from the lane whose ray it helps (share.cuh).
+struct BatchLane {
+    const float4*& nodes;
+    const float4*& prims;
+    void*& out;
+    uint32_t& mode;
+    __device__ __forceinline__ void take(uint32_t src) {
+        nodes = reinterpret_cast<const float4*>(__shfl_sync(0xffffffffu, (unsigned long long)nodes, src));
+        prims = reinterpret_cast<const float4*>(__shfl_sync(0xffffffffu, (unsigned long long)prims, src));
+        out = reinterpret_cast<void*>(__shfl_sync(0xffffffffu, (unsigned long long)out, src));
+        mode = __shfl_sync(0xffffffffu, mode, src);
+    }
+    __device__ __forceinline__ bool any() const { return mode != 0; }
 };
 
 template <int LAYOUT>
@@ -56,7 +87,14 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
     RayState r;
     BestHit best;
     uint32_t unused = 0;
+    // work sharing once the queue is drained (share.cuh)
+    uint32_t link = lane;
     for (;;) {
+        if (queue_done && __ballot_sync(0xffffffffu, !alive || (link & (kLinkWait | kLinkMerge))) != 0) {
+            BatchLane lane_item{nodes, prims, out, mode};
+            share_tail<kSharePerLane>(lane, lower, link, alive, ray, r, best, st, next, lane_item,
+                                      [&](bool occ) { write_result(out, mode, ray, r, best, occ); });
+        }
         const uint32_t idle = __ballot_sync(0xffffffffu, !alive);
         const uint32_t nidle = __popc(idle);
         if (!queue_done && nidle != 0 && (nidle >= a.refill_lanes || nidle == 32)) {
@@ -114,7 +152,7 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         }
         if (__ballot_sync(0xffffffffu, alive) == 0)
             break;
-        if (alive) {
+        if (alive && !(link & (kLinkWait | kLinkMerge))) {
             bool overflow = false;
             while (next >= 0 && next != kRefDone)
                 next = visit_node<LAYOUT, false>(nodes, next, r, best, st, overflow, unused);
@@ -128,16 +166,13 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
             if (overflow)
                 atomicOr(a.status, kStatusStackOverflow);
             if (occluded || next == kRefDone) {
-                if (mode) {
-                    __stcs(static_cast<uint32_t*>(out) + ray, occluded ? 1u : 0u);
+                if (queue_done) {
+                    // share_tail writes the ray once no helper of it remains
+                    link |= ((link & 31u) == lane ? kLinkWait : kLinkMerge) | (occluded ? kLinkOcc : 0u);
                 } else {
-                    const bool hit = best.t < r.tmax_eff;
-                    const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(best.prim))
-                                         : make_float4(IGXRT_NO_HIT, 0.f, 0.f,
-                                                       __uint_as_float(IGXRT_NO_RAY_HIT));
-                    __stcs(static_cast<float4*>(out) + ray, h);
+                    write_result(out, mode, ray, r, best, occluded);
+                    alive = false;
                 }
-                alive = false;
             }
         }
     }

@@ -29,13 +29,16 @@ CUDA-event time per step (L2 flushed between steps), plain kernels with the
 launch shape the engine's autotuner picks for the step; in the sphere step
 the shadow launch is queued IGXRT_TRACE_INDEPENDENT of the bounce launch
 before it (both read only the primary hits), so it may start while the
-bounce launch drains.  batched: the same
-step as one graph-captured persistent launch.  e2e: the same rays through the
-C ABI with pinned host buffers, all host-device traffic inside the timed
-region: the kernels read the rays and write the results in place over
-NVLink-C2C (the default route), and beside it the staged route (copy up,
-trace, copy down).  --impl reference times the CPU transcription of the reference's
-traversal (the oracle's BVH traversal over the same BVH) on all host cores.
+bounce launch drains.  batched: the same step as one graph-captured
+persistent launch.  e2e: the same rays through the C ABI with pinned host
+buffers, all host-device traffic inside the timed region.  The headline
+route passes the pinned arrays to the stream-ordered calls: the kernels read
+the rays and write the results in host memory over NVLink-C2C, with one
+synchronization per step.  Beside it: host-memory calls on the same memory
+(each returns with its results in host memory), and those calls staged
+(copy up, trace, copy down).  --impl reference times the CPU transcription
+of the reference's traversal (the oracle's BVH traversal over the same BVH)
+on all host cores.
 """
 from __future__ import annotations
 
@@ -488,49 +491,56 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     # e2e: the same rays through the C ABI from pinned host buffers
     host = []
     h2d = d2h = 0
-    for name, rays, prev, mode in batches:
-        hr = torch.empty(len(rays) * 8, dtype=torch.float32, pin_memory=True).numpy()
-        hr[:] = rays.view(np.float32).reshape(-1)
-        hp = None
-        if prev is not None:
-            hp = torch.empty(len(prev), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
-            hp[:] = prev
-        ho = (torch.empty(len(rays) * 4, dtype=torch.float32, pin_memory=True).numpy()
-              .view(igx.HIT_DTYPE) if mode == 0
-              else torch.empty(len(rays), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32))
-        host.append((hr.view(igx.RAY_DTYPE), hp, mode, ho))
+    for i, (name, rays, prev, mode) in enumerate(batches):
+        hr = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+        hp = torch.from_numpy(prev.view(np.int32).copy()).pin_memory() if prev is not None else None
+        ho = (torch.empty((len(rays), 4), dtype=torch.float32) if mode == 0
+              else torch.empty(len(rays), dtype=torch.int32)).pin_memory()
+        host.append((hr, hp, mode, ho, indep[i]))
         h2d += len(rays) * RAY_BYTES + (len(prev) * PREV_BYTES if prev is not None else 0)
         d2h += len(rays) * (HIT_BYTES if mode == 0 else OCC_BYTES)
 
-    def e2e_step():
-        for hr, hp, mode, ho in host:
-            if mode == 0:
-                ctx.trace_closest(scene, hr, hp, out=ho)
-            else:
-                ctx.trace_any(scene, hr, hp, out=ho)
+    def e2e_async_step():
+        # pinned tensors take the stream-ordered call: the kernels read the
+        # rays and write the results in host memory, one synchronization per
+        # step (the shadow launch independent of the bounce launch, as above)
+        for hr, hp, mode, ho, ind in host:
+            f = ctx.trace_closest if mode == 0 else ctx.trace_any
+            f(scene, hr, hp, out=ho, independent=ind)
+        stream.synchronize()
 
-    def e2e_ms_per_step():
+    def e2e_host_call_step():
+        # numpy views of the same pinned memory: IGXRT_TRACE_HOST_MEMORY calls,
+        # each returning once its results are in host memory
+        for hr, hp, mode, ho, _ in host:
+            r = hr.numpy().view(igx.RAY_DTYPE).reshape(-1)
+            pv = hp.numpy().view(np.uint32) if hp is not None else None
+            if mode == 0:
+                ctx.trace_closest(scene, r, pv, out=ho.numpy().view(igx.HIT_DTYPE).reshape(-1))
+            else:
+                ctx.trace_any(scene, r, pv, out=ho.numpy().view(np.uint32))
+
+    def e2e_ms_per_step(step_fn):
         for _ in range(args.warmup):
-            e2e_step()
+            step_fn()
         times = []
         for _ in range(args.steps):
             flush.fill_(0.0)  # no ray or result of the last step stays in L2
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            e2e_step()
+            step_fn()
             times.append(time.perf_counter() - t0)
         spread.append((round(1000 * min(times), 3), round(1000 * max(times), 3)))
         return max_over_ranks(1000 * statistics.mean(times), dev)
 
     spread = []  # (fastest, slowest) step of each route, ms
-    # default route: the kernels read the pinned rays and write the results
-    # in place over NVLink-C2C; then the same calls staged through device
-    # buffers (IGXRT_TRACE_STAGED: copy up, trace, copy down)
-    e2e_ms = e2e_ms_per_step()
-    ctx.stage_host_arrays = True
-    staged_ms = e2e_ms_per_step()
+    e2e_ms = e2e_ms_per_step(e2e_async_step)
+    host_call_ms = e2e_ms_per_step(e2e_host_call_step)
+    ctx.stage_host_arrays = True  # IGXRT_TRACE_STAGED: copy up, trace, copy down
+    staged_ms = e2e_ms_per_step(e2e_host_call_step)
     ctx.stage_host_arrays = False
     e2e_value = world * total_rays / (e2e_ms / 1e3) / 1e6
+    mrays = lambda ms: round(world * total_rays / (ms / 1e3) / 1e6, 3)
 
     if rank != 0:
         return
@@ -555,10 +565,16 @@ def run_engine(args, rank: int, world: int, local_rank: int):
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3),
                     "ms_min_max": spread[0],
-                    "route": "pinned host arrays read and written in place by the kernels (NVLink-C2C)",
-                    "staged": {"value": round(world * total_rays / (staged_ms / 1e3) / 1e6, 3),
-                               "ms_per_step": round(staged_ms, 3), "ms_min_max": spread[1],
-                               "route": "IGXRT_TRACE_STAGED: copy up, trace, copy down"}},
+                    "route": "pinned host tensors through the stream-ordered calls: the kernels read "
+                             "the rays and write the results in host memory over NVLink-C2C; one "
+                             "synchronization per step",
+                    "host_calls": {"value": mrays(host_call_ms), "ms_per_step": round(host_call_ms, 3),
+                                   "ms_min_max": spread[1],
+                                   "route": "IGXRT_TRACE_HOST_MEMORY calls on the same pinned memory, "
+                                            "each returning with its results in host memory"},
+                    "staged": {"value": mrays(staged_ms), "ms_per_step": round(staged_ms, 3),
+                               "ms_min_max": spread[2],
+                               "route": "IGXRT_TRACE_STAGED: copy up, trace, copy down, per call"}},
             "gpu_launches": args.steps * nb,
             "clocks": clk,
             "wall_s_timed_region": round(wall, 3)}

@@ -36,6 +36,12 @@ def _is_cuda_tensor(x) -> bool:
     return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
 
 
+def _is_addressable_tensor(x) -> bool:
+    """A tensor the kernels can read and write in place: CUDA memory, or
+    pinned host memory (reached over NVLink-C2C on a GB300)."""
+    return torch is not None and isinstance(x, torch.Tensor) and (x.is_cuda or x.is_pinned())
+
+
 def as_triangles(tris) -> np.ndarray:
     """Accepts a TRIANGLE_DTYPE array, or (N,3,3) / (N,9) vertex positions."""
     a = np.asarray(tris)
@@ -401,16 +407,23 @@ class Context:
         return C.c_void_p(0)
 
     def _trace(self, scene: Scene, rays, prev_hit, mode: int, stream, out=None, independent=False):
+        """CUDA or pinned CPU tensors: the stream-ordered device call (returns
+        once queued; pinned arrays are read and written in place).  numpy
+        arrays: IGXRT_TRACE_HOST_MEMORY (returns once the results are in host
+        memory)."""
         fn = lib().igxrt_trace_closest if mode == 0 else lib().igxrt_trace_any
-        if _is_cuda_tensor(rays):
+        if _is_addressable_tensor(rays):
             assert rays.dtype == torch.float32 and rays.is_contiguous() and rays.shape[-1] == 8
             n = rays.shape[0]
             if out is None:
-                out = (torch.empty((n, 4), dtype=torch.float32, device=rays.device) if mode == 0
-                       else torch.empty(n, dtype=torch.int32, device=rays.device))
+                shape = (n, 4) if mode == 0 else (n,)
+                dtype = torch.float32 if mode == 0 else torch.int32
+                out = (torch.empty(shape, dtype=dtype, device=rays.device) if rays.is_cuda
+                       else torch.empty(shape, dtype=dtype).pin_memory())
+            assert _is_addressable_tensor(out) and out.is_contiguous()
             prev_ptr = None
             if prev_hit is not None:
-                assert _is_cuda_tensor(prev_hit) and prev_hit.dtype == torch.int32
+                assert _is_addressable_tensor(prev_hit) and prev_hit.dtype == torch.int32
                 prev_ptr = prev_hit.data_ptr()
             st = fn(self._h, scene.handle, rays.data_ptr(), prev_ptr, n, out.data_ptr(),
                     TRACE_INDEPENDENT if independent else 0, self._stream(stream, True))

@@ -316,3 +316,26 @@ def test_independent_launches_and_queue_slot_reuse(ctx):
     assert got_h.tobytes() == expect_hits.tobytes()
     assert np.array_equal(got_o, expect_occ)
     assert expect_occ.any() and not expect_occ.all()
+
+
+def test_pinned_tensors_take_the_stream_ordered_path(ctx):
+    """Pinned CPU tensors are addressable by the kernels: the call queues the
+    launch on the stream (no host synchronization) and the kernel reads the
+    rays and writes the results in host memory; after a stream
+    synchronization they equal the host-memory call's."""
+    import torch
+
+    tris = scenes.random_triangles(20000, 97, mu=math.log(0.01))
+    rays = scenes.incoherent_rays(200_000, 98)
+    rays["tmax"] = np.where(np.arange(len(rays)) % 2 == 0, 0.3, 3.0e38).astype(np.float32)
+    scene = ctx.create_scene(tris)
+    h_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
+    hits = ctx.trace_closest(scene, h_rays)
+    assert hits.is_pinned() and not hits.is_cuda
+    prev = torch.from_numpy(np.arange(len(rays), dtype=np.int32) % 20000).pin_memory()
+    occ = ctx.trace_any(scene, h_rays, prev, independent=True)
+    torch.cuda.synchronize()
+    assert hits.numpy().view(HIT_DTYPE).reshape(-1).tobytes() == scene.trace_geometry(rays).tobytes()
+    expect = scene.trace_occlusion(rays, prev.numpy().view(np.uint32))
+    assert np.array_equal(occ.numpy().view(np.uint32), expect)
+    assert expect.any() and not expect.all()

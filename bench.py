@@ -981,7 +981,8 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         n = w * h
         line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,
                      dict(cfg, workload="gbuffer_sphere_1m_1080p", rays_per_step=n),
-                     roofline=_roofline(b, ms, f"gbuffer_kernel<{LAYOUT_NAMES[layout]}>"),
+                     roofline=_roofline(b, ms, f"gbuffer_kernel<{LAYOUT_NAMES[layout]}>",
+                                        traffic_from_profiles("gbuffer_sphere_1m_1080p", "gbuffer", layout)),
                      e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                           "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 32 * n,
                           "ms_per_step": round(e2e_ms, 3)},
@@ -1038,7 +1039,8 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,
                      dict(cfg, workload="shadowmask_sphere_1m_1080p_1_sample", rays_per_step=n,
                           light=list(scenes.SPHERE_LIGHT)),
-                     roofline=_roofline(b, ms, f"shadow pass: compact + trace_kernel<{LAYOUT_NAMES[layout]},any> + pack"),
+                     roofline=_roofline(b, ms, f"shadow pass: compact + trace_kernel<{LAYOUT_NAMES[layout]},any> + pack",
+                                        traffic_from_profiles("shadowmask_sphere_1m_1080p_1_sample", "pass", layout)),
                      e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                           "h2d_bytes_per_step": 36 * w * h, "d2h_bytes_per_step": 4 * words,
                           "ms_per_step": round(e2e_ms, 3)},
@@ -1105,7 +1107,8 @@ def run_mixed_bench(args, rank: int, world: int, local_rank: int):
            "launch": ctx.launch_params, "bvh_build_s": round(build_s, 2),
            "l2": "256 MiB buffer written between timed steps"}
     line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms, cfg,
-                 roofline=_roofline(b, ms, f"trace_kernel<{LAYOUT_NAMES[layout]},closest,mixed>"),
+                 roofline=_roofline(b, ms, f"trace_kernel<{LAYOUT_NAMES[layout]},closest,mixed>",
+                                    traffic_from_profiles(cfg["workload"], "mixed", layout)),
                  e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                       "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 16 * n,
                       "ms_per_step": round(e2e_ms, 3)},
@@ -1192,7 +1195,8 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
            "frames": len(frames), "host_sah_build_s": round(host_build_s, 3),
            "l2": "256 MiB buffer written between timed steps"}
     line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms, cfg,
-                 roofline=_roofline(b, trace_only, f"trace_kernel<{LAYOUT_NAMES[layout]},closest> (frame rays)"),
+                 roofline=_roofline(b, trace_only, f"trace_kernel<{LAYOUT_NAMES[layout]},closest> (frame rays)",
+                                    traffic_from_profiles(cfg["workload"], "frame", layout)),
                  frame={"refit_ms": round(refit_only, 4), "trace_ms": round(trace_only, 4),
                         "refit_plus_trace_ms": round(ms, 4),
                         "gpu_rebuild_plus_trace_ms": round(rebuild_ms, 4),

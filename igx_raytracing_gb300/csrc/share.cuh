@@ -37,11 +37,13 @@ struct NoLaneExtra {
 // One round of tail work sharing, run by the whole warp between traversal
 // phases.  `extra` holds lane state a helper must copy from its victim
 // (take(src) reads it from lane src; lanes that take nothing read their
-// own); `finish(occluded)` writes the lane's ray.
+// own); `finish(occluded)` writes the lane's ray; `no_hit` is the value of
+// BestHit.prim before a first hit (0, or the priority code of mixed
+// scenes, whose merges then compare (t, priority) like their leaves do).
 template <int MODE, class Extra, class Finish>
 __device__ __forceinline__ void share_tail(uint32_t lane, uint32_t lower, uint32_t& link, bool& alive,
                                            uint32_t& ray, RayState& r, BestHit& best, TraversalStack& st,
-                                           int32_t& next, Extra& extra, Finish finish) {
+                                           int32_t& next, Extra& extra, Finish finish, uint32_t no_hit = 0u) {
     constexpr bool CLOSEST = MODE != kShareAny;  // per-lane mode merges both ways
     constexpr uint32_t FULL = 0xffffffffu;
     // 1. finished helpers hand their best hit (or occluder) to the owner
@@ -155,7 +157,7 @@ __device__ __forceinline__ void share_tail(uint32_t lane, uint32_t lower, uint32
         best.t = r.tmax_eff;
         best.u = 0.f;
         best.v = 0.f;
-        best.prim = 0u;
+        best.prim = no_hit;
         best.tcull = vtc;
         next = (int32_t)e.x;
         st.sp = 0;

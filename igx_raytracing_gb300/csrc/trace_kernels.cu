@@ -114,7 +114,7 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
     BestHit best;
     // work sharing in the tail (share_tail); the instrumented kernels keep
     // the single-lane order their fetch counts describe
-    constexpr bool STEAL = !COUNT && !MIXED;
+    constexpr bool STEAL = !COUNT;
     uint32_t link = lane;
     for (;;) {
         if (STEAL && queue_done &&
@@ -122,7 +122,8 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
             NoLaneExtra none;
             share_tail<ANY ? kShareAny : kShareClosest>(
                 lane, lower, link, alive, ray, r, best, st, next, none,
-                [&](bool occ) { finish_ray<ANY, false, false>(a, ray, r, best, occ, 0, 0); });
+                [&](bool occ) { finish_ray<ANY, false, MIXED>(a, ray, r, best, occ, 0, 0); },
+                MIXED ? kPrioNone : 0u);
         }
         const uint32_t idle = __ballot_sync(0xffffffffu, !alive);
         const uint32_t nidle = __popc(idle);

@@ -71,7 +71,8 @@ def test_small_workload_all_rays_vs_brute_force(ctx):
 
 
 @pytest.mark.parametrize("block,depth,packet", [(32, 0, 32), (64, 8, 64), (128, 16, 64),
-                                                (256, 32, 128), (128, 64, 4096), (256, 0, 32)])
+                                                (256, 32, 128), (128, 64, 4096), (256, 0, 32),
+                                                (128, 2, 32)])
 @pytest.mark.parametrize("layout", LAYOUTS)
 def test_launch_shapes_agree(params, block, depth, packet, layout):
     ctx = params

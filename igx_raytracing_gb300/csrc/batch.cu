@@ -61,7 +61,6 @@ struct BatchLane {
         out = reinterpret_cast<void*>(__shfl_sync(0xffffffffu, (unsigned long long)out, src));
         mode = __shfl_sync(0xffffffffu, mode, src);
     }
-    __device__ __forceinline__ bool any() const { return mode != 0; }
 };
 
 template <int LAYOUT>

@@ -9,9 +9,9 @@ namespace igxrt {
 //
 // After a warp finds the queue empty its lanes finish the rays they hold, and
 // the warp runs until its slowest ray is done while finished lanes idle.
-// From then on an idle lane takes the bottom entry (the oldest, largest
-// pending subtree) of a busy lane's stack and traverses it for the same ray,
-// as a helper of the lane that owns the ray.  A helper keeps its own best hit
+// From then on idle lanes take the bottom entries (the oldest, largest
+// pending subtrees) of busy lanes' stacks and traverse them for the same
+// rays, as helpers of the lanes that own the rays.  A helper keeps its own best hit
 // and stack; when its subtrees are done it hands the best hit to the owner,
 // and the owner writes the ray's result once its own traversal is over and no
 // helper of its ray remains.  The result equals the single-lane traversal's:
@@ -25,13 +25,12 @@ constexpr uint32_t kLinkMerge = 1u << 9;  // helper: subtrees done, best hit to 
 constexpr uint32_t kLinkOcc = 1u << 10;   // any-hit: an occluder was found
 
 // Query modes of share_tail: every lane the same (closest or any hit), or
-// per lane (`extra.any()`, the batch kernel).
+// either per lane (the batch kernel: the merge then handles both).
 constexpr int kShareClosest = 0, kShareAny = 1, kSharePerLane = 2;
 
 // No per-lane state beyond the ray (the plain trace kernels).
 struct NoLaneExtra {
     __device__ __forceinline__ void take(uint32_t) {}
-    __device__ __forceinline__ bool any() const { return false; }
 };
 
 // One round of tail work sharing, run by the whole warp between traversal

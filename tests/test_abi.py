@@ -59,3 +59,29 @@ def test_create_without_gpu_reports_cuda_error(engine_lib):
     h = C.c_void_p()
     assert engine_lib.igxrt_create(0, C.byref(h)) == 2
     assert not h.value
+
+
+def test_python_constants_match_the_header():
+    """Every #define the Python binding restates (flags, layouts, modes,
+    sentinels, the static path's limits) has the header's value."""
+    text = open(HEADER).read()
+    defines = {}
+    for name, value in re.findall(r"#define\s+(IGXRT_[A-Z0-9_]+)\s+([^\s/]+)", text):
+        defines[name] = value
+    as_int = lambda v: int(v.rstrip("uU"), 0)
+    pairs = {"IGXRT_TRACE_HOST_MEMORY": _capi.TRACE_HOST_MEMORY, "IGXRT_TRACE_STAGED": _capi.TRACE_STAGED,
+             "IGXRT_TRACE_INDEPENDENT": _capi.TRACE_INDEPENDENT, "IGXRT_LAYOUT_BVH2": _capi.LAYOUT_BVH2,
+             "IGXRT_LAYOUT_BVH4": _capi.LAYOUT_BVH4, "IGXRT_LAYOUT_BVH8": _capi.LAYOUT_BVH8,
+             "IGXRT_LAYOUT_COUNT": _capi.LAYOUT_COUNT, "IGXRT_MODE_CLOSEST": _capi.MODE_CLOSEST,
+             "IGXRT_MODE_ANY": _capi.MODE_ANY, "IGXRT_NO_RAY_HIT": _capi.NO_RAY_HIT}
+    for name, value in pairs.items():
+        assert name in defines, name
+        assert as_int(defines[name]) == value, name
+    import numpy as np
+
+    assert np.float32(defines["IGXRT_NO_HIT"].rstrip("fF")) == _capi.NO_HIT
+    assert as_int(defines["IGXRT_STATIC_MAX_RAYS"]) == _capi.STATIC_MAX_RAYS
+    m = re.search(r"#define\s+IGXRT_STATIC_SCRATCH_BYTES\s+\((\d+)u\s*<<\s*(\d+)\)", text)
+    assert m and int(m.group(1)) << int(m.group(2)) == _capi.STATIC_SCRATCH_BYTES
+    flags = [_capi.TRACE_HOST_MEMORY, _capi.TRACE_STAGED, _capi.TRACE_INDEPENDENT]
+    assert all(f & (f - 1) == 0 for f in flags) and len(set(flags)) == 3  # distinct bits

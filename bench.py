@@ -1237,6 +1237,7 @@ def main():
     if world > 1:
         import torch
 
+        torch.cuda.set_device(local_rank)  # each rank's collectives on its own GPU
         torch.distributed.init_process_group("nccl")
     if args.workload == "batch":
         run_batch_bench(args, rank, world, local_rank)

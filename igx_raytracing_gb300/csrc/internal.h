@@ -55,11 +55,19 @@ constexpr uint32_t kNoSource = 0xffffffffu;
 // byte whose decodings fmaf(q, 2^exp, origin) still enclose its box.  The
 // decoding is monotone in q, byte 0 decodes to origin <= every slot's lo and
 // byte 255 to at least hi, so both searches end inside [0, 255].
+// The loops settle on the smallest e in [-126, 127] with
+// fmaf(255, 2^e, lo) >= hi (127 if none); that predicate only strengthens as
+// e grows, so the result does not depend on the starting estimate, which
+// binary32 arithmetic gives within a step or two (a GPU's binary64 is slow).
 IGXRT_HD inline int bvh8_exponent(float lo, float hi) {
     int k = 0;
-    const double ext = (double)hi - (double)lo;
-    if (ext > 0.0)
-        frexp(ext, &k);
+    const float ext = hi - lo;
+    if (ext > 0.f) {
+        if (ext <= 3.4028235e38f)
+            frexpf(ext, &k);
+        else
+            k = 128;
+    }
     int e = k - 8 < -126 ? -126 : (k - 8 > 127 ? 127 : k - 8);
     while (e < 127 && fmaf(255.f, ldexpf(1.f, e), lo) < hi)
         ++e;
@@ -68,13 +76,16 @@ IGXRT_HD inline int bvh8_exponent(float lo, float hi) {
     return e;
 }
 
+// The loops settle on the largest byte a whose decoding fmaf(a, 2^exp,
+// origin) is at most lo and the smallest byte b whose decoding is at least hi
+// (decodings grow with the byte), whatever the starting estimate; binary32
+// estimates land within a step or two.
 IGXRT_HD inline void bvh8_quantize(float origin, int exp, float lo, float hi, uint8_t& qlo, uint8_t& qhi) {
     const float s = ldexpf(1.f, exp);
-    const double step = ldexp(1.0, exp);
-    double ea = floor(((double)lo - (double)origin) / step);
-    double eb = ceil(((double)hi - (double)origin) / step);
-    int a = (int)(ea < 0.0 ? 0.0 : (ea > 255.0 ? 255.0 : ea));
-    int b = (int)(eb < 0.0 ? 0.0 : (eb > 255.0 ? 255.0 : eb));
+    const float ea = floorf(ldexpf(lo - origin, -exp));
+    const float eb = ceilf(ldexpf(hi - origin, -exp));
+    int a = (int)(ea > 0.f ? (ea < 255.f ? ea : 255.f) : 0.f);  // NaN -> 0
+    int b = (int)(eb > 0.f ? (eb < 255.f ? eb : 255.f) : 0.f);
     while (a > 0 && fmaf((float)a, s, origin) > lo)
         --a;
     while (a < 255 && fmaf((float)(a + 1), s, origin) <= lo)

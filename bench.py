@@ -1190,6 +1190,9 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
     nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
     n = len(rays)
     b = algorithmic_bytes(nf, pf, 0, False, layout)
+    # a frame: the refit's scan, records, nodes and BVH8 passes, then the trace
+    si = scene.info
+    refit_launches = 2 + (si["bvh2_nodes"] + si["bvh4_nodes"] > 0) + (si["bvh8_nodes"] > 0) + 1
     cfg = {"workload": "dynamic_sphere_1m_refit_1080p_primary", "triangles": len(tris),
            "rays_per_step": n, "layout": LAYOUT_NAMES[layout], "launch": ctx.launch_params,
            "frames": len(frames), "host_sah_build_s": round(host_build_s, 3),
@@ -1205,7 +1208,7 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
                  e2e={"value": round(world * n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
                       "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0, "ms_per_step": round(ms, 4),
                       "note": "positions and rays resident: a frame's geometry arrives from a device kernel"},
-                 gpu_launches=args.steps * 4, clocks=clk)
+                 gpu_launches=args.steps * refit_launches, clocks=clk)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -46,6 +46,12 @@ constexpr uint32_t kNoSource = 0xffffffffu;
 #else
 #define IGXRT_HD
 #endif
+// Full unrolling in device code (keeps small fixed-size arrays in registers).
+#ifdef __CUDA_ARCH__
+#define IGXRT_UNROLL _Pragma("unroll")
+#else
+#define IGXRT_UNROLL
+#endif
 
 // BVH8 quantization, compiled for the host builder and refit and for the GPU
 // refit from this one definition so both produce the same bytes.  A node's
@@ -104,9 +110,12 @@ IGXRT_HD inline void bvh8_quantize(float origin, int exp, float lo, float hi, ui
 IGXRT_HD inline void bvh8_quantize_node(const igxrt_bvh2_node* nodes2, const uint32_t* src,
                                         igxrt_bvh8_node& n) {
     float lo[8][3], hi[8][3];
+    bool used[8];
     float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    IGXRT_UNROLL
     for (int c = 0; c < 8; ++c) {
-        if (src[c] == kNoSource)
+        used[c] = src[c] != kNoSource;
+        if (!used[c])
             continue;
         const igxrt_bvh2_node& m = nodes2[src[c] >> 1];
         const int s = (int)(src[c] & 1u);
@@ -119,25 +128,27 @@ IGXRT_HD inline void bvh8_quantize_node(const igxrt_bvh2_node* nodes2, const uin
         hi[c][1] = y[1];
         lo[c][2] = z[0];
         hi[c][2] = z[1];
+        IGXRT_UNROLL
         for (int a = 0; a < 3; ++a) {
             nlo[a] = lo[c][a] < nlo[a] ? lo[c][a] : nlo[a];
             nhi[a] = nhi[a] < hi[c][a] ? hi[c][a] : nhi[a];
         }
     }
-    int e[3];
+    IGXRT_UNROLL
     for (int a = 0; a < 3; ++a) {
-        e[a] = bvh8_exponent(nlo[a], nhi[a]);
+        const int e = bvh8_exponent(nlo[a], nhi[a]);
         n.origin[a] = nlo[a];
-        n.exp[a] = (int8_t)e[a];
-    }
-    uint8_t* q[3][2] = {{n.lo_x, n.hi_x}, {n.lo_y, n.hi_y}, {n.lo_z, n.hi_z}};
-    for (int c = 0; c < 8; ++c)
-        for (int a = 0; a < 3; ++a) {
-            if (src[c] == kNoSource)
-                q[a][0][c] = q[a][1][c] = 0;
+        n.exp[a] = (int8_t)e;
+        uint8_t* qlo = a == 0 ? n.lo_x : (a == 1 ? n.lo_y : n.lo_z);
+        uint8_t* qhi = a == 0 ? n.hi_x : (a == 1 ? n.hi_y : n.hi_z);
+        IGXRT_UNROLL
+        for (int c = 0; c < 8; ++c) {
+            if (used[c])
+                bvh8_quantize(nlo[a], e, lo[c][a], hi[c][a], qlo[c], qhi[c]);
             else
-                bvh8_quantize(nlo[a], e[a], lo[c][a], hi[c][a], q[a][0][c], q[a][1][c]);
+                qlo[c] = qhi[c] = 0;
         }
+    }
 }
 
 // Thread-safe formatted message helper.

@@ -2,7 +2,7 @@
 //
 // The reference re-uploads its moving spheres every frame and traces them with
 // a linear loop (test/scene/niels_scene.cpp:61-70, res/shaders/trace.glsl:22-46);
-// over a BVH, moved geometry needs the node boxes to follow.  Three passes on
+// over a BVH, moved geometry needs the node boxes to follow.  Four passes on
 // the caller's stream:
 //   1. scan: bounds of every object, max |coordinate| (which sets the padding)
 //      and the scene box, reduced per block, then one atomicMax per block and
@@ -14,7 +14,9 @@
 //      node's slot boxes, then climbs through the parent links.  At each parent
 //      an atomic arrival counter lets only the thread of the last interior child
 //      go on, so every node is written once, after all of its children.  Nothing
-//      waits on another thread: a thread either continues or exits.
+//      waits on another thread: a thread either continues or exits;
+//   4. BVH8: every compressed node re-quantized from the BVH2 boxes its slots
+//      were built from (eight lanes per node).
 // Boxes follow the host builder exactly (same min/max argument order, padded by
 // max(2^-18 * max|coordinate|, 1e-30)), so the GPU refit equals igxrt_bvh_refit
 // bit for bit.
@@ -129,25 +131,52 @@ __global__ void __launch_bounds__(kScanBlock) refit_scan_kernel(RefitArgs a) {
     scan_objects<false>(a.obj, a.state);
 }
 
-// Pass 2: primitive records and the scene's triangle and plane copies.
+// Pass 2: primitive records and the scene's triangle and plane copies.  The
+// scene's buffers are 256-byte aligned; 16-byte loads and stores are used
+// wherever the caller's buffer is 16-byte aligned too.
 __global__ void refit_records_kernel(RefitArgs a) {
     if (a.state[kWordBad])
         return;
     const SceneObjects& o = a.obj;
     const uint32_t n = o.count();
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t span = max(n, 4 * o.np);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < span; i += stride) {
-        if (i < n) {
-            igxrt_prim_record r = a.prims[i];
-            fill_record(o, r.prim, r);
-            a.prims[i] = r;
+    const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool tris16 = (reinterpret_cast<uintptr_t>(o.tris) & 15u) == 0;
+    float4* rec = reinterpret_cast<float4*>(a.prims);
+    for (uint32_t i = first; i < n; i += stride) {
+        float4 r0 = rec[3 * (size_t)i], r1 = rec[3 * (size_t)i + 1], r2 = rec[3 * (size_t)i + 2];
+        const uint32_t id = __float_as_uint(r0.w);
+        if (id < o.nt && tris16) {
+            const float4* t = reinterpret_cast<const float4*>(o.tris + id);
+            const float4 q0 = __ldg(t), q1 = __ldg(t + 1), q2 = __ldg(t + 2);
+            r0 = make_float4(q0.x, q0.y, q0.z, r0.w);
+            r1 = make_float4(__fsub_rn(q1.x, q0.x), __fsub_rn(q1.y, q0.y), __fsub_rn(q1.z, q0.z), r1.w);
+            r2 = make_float4(__fsub_rn(q2.x, q0.x), __fsub_rn(q2.y, q0.y), __fsub_rn(q2.z, q0.z), r2.w);
+        } else {
+            igxrt_prim_record r;
+            memcpy(&r, &r0, 16);
+            memcpy(reinterpret_cast<char*>(&r) + 16, &r1, 16);
+            memcpy(reinterpret_cast<char*>(&r) + 32, &r2, 16);
+            fill_record(o, id, r);
+            memcpy(&r0, &r, 16);
+            memcpy(&r1, reinterpret_cast<const char*>(&r) + 16, 16);
+            memcpy(&r2, reinterpret_cast<const char*>(&r) + 32, 16);
         }
-        if (i < o.nt)
-            a.scene_tris[i] = o.tris[i];
-        if (i < 4 * o.np)
-            a.scene_planes[i] = o.planes[i];
+        rec[3 * (size_t)i] = r0;
+        rec[3 * (size_t)i + 1] = r1;
+        rec[3 * (size_t)i + 2] = r2;
     }
+    if (tris16) {
+        const float4* src = reinterpret_cast<const float4*>(o.tris);
+        float4* dst = reinterpret_cast<float4*>(a.scene_tris);
+        for (size_t i = first; i < 3 * (size_t)o.nt; i += stride)
+            dst[i] = __ldg(src + i);
+    } else {
+        for (uint32_t i = first; i < o.nt; i += stride)
+            a.scene_tris[i] = o.tris[i];
+    }
+    for (uint32_t i = first; i < 4 * o.np; i += stride)
+        a.scene_planes[i] = o.planes[i];
 }
 
 __device__ Box leaf_box(const RefitArgs& a, int32_t ref, float pad) {
@@ -193,6 +222,15 @@ __device__ void refit_node(const RefitArgs& a, typename NodeOps<LAYOUT>::Node* n
     }
 }
 
+// Arrival at a parent: an acquire-release add at GPU scope, so this node's
+// boxes are visible before the count moves, and the thread that sees the last
+// arrival sees every sibling's boxes.
+__device__ __forceinline__ uint32_t arrive_at(uint32_t* counter) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
+    return old;
+}
+
 template <int LAYOUT>
 __device__ void refit_climb(const RefitArgs& a, uint32_t node, float pad) {
     using Node = typename NodeOps<LAYOUT>::Node;
@@ -206,11 +244,9 @@ __device__ void refit_climb(const RefitArgs& a, uint32_t node, float pad) {
         const uint32_t p = parents[node];
         if (p == kNoParent)
             return;
-        __threadfence();  // this node's boxes before the arrival
         const uint32_t need = (uint32_t)interior_children<LAYOUT>(nodes + p);
-        if (atomicAdd(arrive + p, 1u) + 1u != need)
+        if (arrive_at(arrive + p) + 1u != need)
             return;  // a sibling's thread is still below; it will come up
-        __threadfence();  // the siblings' boxes after their arrivals
         node = p;
     }
 }
@@ -228,16 +264,82 @@ __global__ void refit_nodes_kernel(RefitArgs a) {
 }
 
 // Pass 4: every BVH8 node re-quantized from the refit BVH2 boxes of its
-// slots (the host refit calls the same bvh8_quantize_node).
-__global__ void refit_bvh8_kernel(RefitArgs a) {
+// slots, eight lanes per node, one per slot.  The node's bounds are reduced
+// across the eight lanes with the lower slot as the first operand of every
+// comparison, which picks the same element as the host's slot-order loop in
+// bvh8_quantize_node (ties, signed zeros included); each lane then quantizes
+// its own slot with the same bvh8_exponent / bvh8_quantize, and the bytes are
+// packed into words with shuffles and stored as four 16-byte words.
+__global__ void __launch_bounds__(128) refit_bvh8_kernel(RefitArgs a) {
     if (a.state[kWordBad])
         return;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.n8)
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t node = t >> 3;
+    const uint32_t slot = (uint32_t)(t & 7u);
+    const bool live = node < a.n8;  // the same for the eight lanes of a node
+    const uint32_t src = live ? a.src8[8 * node + slot] : kNoSource;
+    const bool used = src != kNoSource;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    if (used) {
+        const float4* q = reinterpret_cast<const float4*>(static_cast<const igxrt_bvh2_node*>(a.nodes2) +
+                                                          (src >> 1));
+        const uint32_t s = src & 1u;
+        const float4 xy = q[s];  // c{s}_x, c{s}_y
+        const float2 z = reinterpret_cast<const float2*>(q + 2)[s];  // c{s}_z
+        lo[0] = xy.x, hi[0] = xy.y, lo[1] = xy.z, hi[1] = xy.w, lo[2] = z.x, hi[2] = z.y;
+    }
+    float nlo[3], nhi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        nlo[k] = lo[k];
+        nhi[k] = hi[k];
+    }
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float olo = __shfl_down_sync(0xffffffffu, nlo[k], d, 8);
+            const float ohi = __shfl_down_sync(0xffffffffu, nhi[k], d, 8);
+            nlo[k] = olo < nlo[k] ? olo : nlo[k];
+            nhi[k] = nhi[k] < ohi ? ohi : nhi[k];
+        }
+    uint32_t word[6];  // lo_x, hi_x, lo_y, hi_y, lo_z, hi_z: this lane's byte in place
+    int e[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        nlo[k] = __shfl_sync(0xffffffffu, nlo[k], 0, 8);
+        nhi[k] = __shfl_sync(0xffffffffu, nhi[k], 0, 8);
+        e[k] = live ? bvh8_exponent(nlo[k], nhi[k]) : 0;
+        uint8_t ql = 0, qh = 0;
+        if (used)
+            bvh8_quantize(nlo[k], e[k], lo[k], hi[k], ql, qh);
+        word[2 * k] = (uint32_t)ql << (8 * (slot & 3u));
+        word[2 * k + 1] = (uint32_t)qh << (8 * (slot & 3u));
+    }
+    uint32_t half[2][6];  // [slots 0-3 | slots 4-7][array]
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        uint32_t w = word[k];
+        w |= __shfl_xor_sync(0xffffffffu, w, 1, 8);
+        w |= __shfl_xor_sync(0xffffffffu, w, 2, 8);
+        const uint32_t other = __shfl_xor_sync(0xffffffffu, w, 4, 8);
+        half[0][k] = slot < 4 ? w : other;
+        half[1][k] = slot < 4 ? other : w;
+    }
+    if (!live || slot > 3)
         return;
-    igxrt_bvh8_node n = a.nodes8[i];
-    bvh8_quantize_node(static_cast<const igxrt_bvh2_node*>(a.nodes2), a.src8 + 8 * (size_t)i, n);
-    a.nodes8[i] = n;
+    uint4* out = reinterpret_cast<uint4*>(a.nodes8 + node);
+    uint4 v;
+    if (slot == 0) {
+        const uint32_t valid = out[0].w & 0xff000000u;  // kept; the exponents are rewritten
+        v = make_uint4(__float_as_uint(nlo[0]), __float_as_uint(nlo[1]), __float_as_uint(nlo[2]),
+                       (uint32_t)(uint8_t)e[0] | (uint32_t)(uint8_t)e[1] << 8 | (uint32_t)(uint8_t)e[2] << 16 |
+                           valid);
+    } else {
+        const int k = 2 * (int)(slot - 1);  // slot 1: lo_x, hi_x; 2: lo_y, hi_y; 3: lo_z, hi_z
+        v = make_uint4(half[0][k], half[1][k], half[0][k + 1], half[1][k + 1]);
+    }
+    out[slot] = v;
 }
 
 }  // namespace
@@ -298,7 +400,7 @@ igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igx
     if (nodes)
         refit_nodes_kernel<<<(nodes + 127) / 128, 128, 0, s>>>(a);
     if (a.n8)
-        refit_bvh8_kernel<<<(a.n8 + 127) / 128, 128, 0, s>>>(a);
+        refit_bvh8_kernel<<<(uint32_t)((8 * (uint64_t)a.n8 + 127) / 128), 128, 0, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "refit launch");

@@ -33,6 +33,16 @@ std::string non_finite_message(uint32_t bad_word, uint32_t objects);
 __device__ __forceinline__ float host_min(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float host_max(float a, float b) { return (a < b) ? b : a; }
 
+// Arrival at a parent in a bottom-up climb: an acquire-release add at GPU
+// scope, so this thread's writes are visible before the count moves, and the
+// thread that sees the last arrival sees every sibling's writes.  Returns the
+// count before the add.
+__device__ __forceinline__ uint32_t arrive_at(uint32_t* counter) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
+    return old;
+}
+
 // Order-preserving map of a float to an unsigned word (for atomicMax/Min).
 __device__ __forceinline__ uint32_t order_key(float f) {
     const uint32_t u = __float_as_uint(f);

@@ -188,10 +188,8 @@ __global__ void radix_boxes_kernel(BuildArgs a) {
             atomicOr(a.state + kWordMalformed, 1u);
             return;
         }
-        __threadfence();
-        if (atomicAdd(a.arrive + p, 1u) == 0)
+        if (arrive_at(a.arrive + p) == 0)
             return;  // the sibling's thread computes this node
-        __threadfence();
         Box b = child_box(a, a.kchild[2 * p]);
         b.grow(child_box(a, a.kchild[2 * p + 1]));
         float* o = a.kbox + 6 * (size_t)p;
@@ -317,8 +315,14 @@ __global__ void bvh4_root_kernel(BuildArgs a) {
 }
 
 // One BVH4 level: each frontier BVH2 node becomes a BVH4 node whose slots are
-// its descendants, opened largest-area-first until four slots are used.
+// its descendants, opened largest-area-first until four slots are used.  The
+// levels are chained by programmatic dependent launch: the next level's blocks
+// are scheduled as soon as this one starts, and its griddepcontrol.wait
+// returns once this grid has finished and its writes are visible, so the
+// (mostly empty) deep levels cost no launch gap.
 __global__ void emit4_level_kernel(BuildArgs a, int level) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
     const uint32_t count = a.state[kWordLevels + level];
     const uint2* in = a.frontier[level & 1];
     uint2* out = a.frontier[(level + 1) & 1];
@@ -425,11 +429,9 @@ __global__ void stack_bound_kernel(BuildArgs a, uint32_t count) {
                 a.state[kWordDepth] = a.depth_v[node];
             return;
         }
-        __threadfence();
         const uint32_t need = (uint32_t)interior_children<LAYOUT>(nodes + p);
-        if (atomicAdd(a.arrive + p, 1u) + 1u != need)
+        if (arrive_at(a.arrive + p) + 1u != need)
             return;
-        __threadfence();
         node = p;
     }
 }
@@ -561,9 +563,19 @@ igxrt_status igxrt_scene_create_gpu(igxrt_context* ctx, const igxrt_scene_desc* 
             return cuda_fail(ctx, e, "node compaction");
         emit2_kernel<<<blocks(n - 1), threads, 0, s>>>(a);
         bvh4_root_kernel<<<1, 1, 0, s>>>(a);
-        const uint32_t level_grid = (uint32_t)std::max(ctx->sm_count, 1) * 4;
-        for (int level = 0; level < kMaxLevels; ++level)
-            emit4_level_kernel<<<level_grid, threads, 0, s>>>(a, level);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((uint32_t)std::max(ctx->sm_count, 1) * 4);
+        cfg.blockDim = dim3(threads);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        for (int level = 0; level < kMaxLevels && e == cudaSuccess; ++level)
+            e = cudaLaunchKernelEx(&cfg, emit4_level_kernel, a, level);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "BVH4 level launch");
     }
     e = cudaGetLastError();
     uint32_t w[kStateWords];

@@ -222,15 +222,6 @@ __device__ void refit_node(const RefitArgs& a, typename NodeOps<LAYOUT>::Node* n
     }
 }
 
-// Arrival at a parent: an acquire-release add at GPU scope, so this node's
-// boxes are visible before the count moves, and the thread that sees the last
-// arrival sees every sibling's boxes.
-__device__ __forceinline__ uint32_t arrive_at(uint32_t* counter) {
-    uint32_t old;
-    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(counter) : "memory");
-    return old;
-}
-
 template <int LAYOUT>
 __device__ void refit_climb(const RefitArgs& a, uint32_t node, float pad) {
     using Node = typename NodeOps<LAYOUT>::Node;

@@ -24,6 +24,7 @@ LAYOUT_COUNT = 3
 TRACE_HOST_MEMORY = 1
 TRACE_STAGED = 2
 TRACE_INDEPENDENT = 4
+TUNE_PLAIN = 1
 STATIC_SCRATCH_BYTES = 16 << 20
 STATIC_MAX_RAYS = 320000
 
@@ -92,7 +93,8 @@ class BatchItem(C.Structure):
 
 class TuneOptions(C.Structure):
     _fields_ = [("reps", C.c_uint32), ("layouts_mask", C.c_uint32), ("cache_path", C.c_char_p),
-                ("class_key", C.c_char_p), ("force", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("class_key", C.c_char_p), ("force", C.c_uint32), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32 * 2)]
 
 
 MODE_CLOSEST = 0

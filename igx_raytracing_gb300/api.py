@@ -23,8 +23,8 @@ import numpy as np
 
 from . import _capi
 from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, RAY_DTYPE, TRACE_HOST_MEMORY,
-                    TRACE_INDEPENDENT, TRACE_STAGED, TRIANGLE_DTYPE, BuildOptions, BvhInfo, IgxrtError,
-                    LaunchParams, check, lib)
+                    TRACE_INDEPENDENT, TRACE_STAGED, TRIANGLE_DTYPE, TUNE_PLAIN, BuildOptions, BvhInfo,
+                    IgxrtError, LaunchParams, check, lib)
 
 try:  # torch is only needed for device-memory calls
     import torch
@@ -572,11 +572,14 @@ class Context:
         return Batch(self, h.value, items)
 
     def autotune(self, items, reps: int = 3, layouts=None, cache_path: Optional[str] = None,
-                 class_key: Optional[str] = None, force: bool = False):
-        """Times candidate launch parameters on the items; returns (params, ms)."""
+                 class_key: Optional[str] = None, force: bool = False, plain: bool = False):
+        """Times candidate launch parameters on the items; returns (params, ms).
+        plain=True times one plain launch per item (IGXRT_TUNE_PLAIN) instead
+        of one batched launch."""
         arr = self.batch_items(items)
         o = _capi.TuneOptions()
         o.reps = reps
+        o.flags = TUNE_PLAIN if plain else 0
         o.layouts_mask = 0 if layouts is None else sum(1 << int(l) for l in layouts)
         o.cache_path = cache_path.encode() if cache_path else None
         o.class_key = class_key.encode() if class_key else None

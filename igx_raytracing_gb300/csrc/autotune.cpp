@@ -4,7 +4,8 @@
 // node layout, packet size, refill threshold, block size and shared stack
 // depth (two rounds; a change is kept only when it is at least 1% faster).
 // Each candidate is timed with CUDA events on a private stream over the
-// caller's items (median of `reps` launches after one warm-up launch).
+// caller's items (median of `reps` repetitions after one warm-up), as one
+// batched launch or, with IGXRT_TUNE_PLAIN, as one plain launch per item.
 // Results can be cached in a text file, one line per (GPU name, class key):
 //     <gpu>|<key>\t<block> <stack> <packet> <layout> <ctas> <refill>\t<ms>
 // The default class key buckets the workload by item count, total rays,
@@ -82,6 +83,7 @@ struct Timer {
     const igxrt_batch_item* items;
     uint32_t count;
     uint32_t reps;
+    bool plain;
     cudaStream_t stream = nullptr;
     BatchItemDev* d_table = nullptr;
     uint32_t* queue = nullptr;
@@ -118,6 +120,8 @@ struct Timer {
 
     // Median launch time in ms, or a negative value if `p` cannot launch.
     float time(const igxrt_launch_params& p) {
+        if (plain)
+            return time_plain(p);
         std::vector<BatchItemDev> table;
         uint32_t packets = 0;
         uint64_t rays = 0;
@@ -143,7 +147,52 @@ struct Timer {
         std::sort(ts.begin(), ts.end());
         return ts[ts.size() / 2];
     }
+
+    // The items as plain launches, one per item in order (IGXRT_TUNE_PLAIN).
+    float time_plain(const igxrt_launch_params& p) {
+        std::vector<float> ts;
+        for (uint32_t r = 0; r < reps + 1; ++r) {
+            cudaEventRecord(e0, stream);
+            for (uint32_t i = 0; i < count; ++i) {
+                const igxrt_batch_item& it = items[i];
+                TraceRequest req{it.scene, it.rays, it.prev_hit, it.count, it.mode,
+                                 it.mode == IGXRT_MODE_CLOSEST ? static_cast<igxrt_hit*>(it.out) : nullptr,
+                                 it.mode == IGXRT_MODE_ANY ? static_cast<uint32_t*>(it.out) : nullptr,
+                                 nullptr, nullptr};
+                if (launch_trace(ctx, req, p, stream) != IGXRT_OK)
+                    return -1.f;
+            }
+            cudaEventRecord(e1, stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess)
+                return -1.f;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0)
+                ts.push_back(ms);
+        }
+        std::sort(ts.begin(), ts.end());
+        return ts[ts.size() / 2];
+    }
 };
+
+// Items a plain-launch tuning can time: scenes of this context, arrays the
+// kernels can address, known modes.
+igxrt_status check_plain_items(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count) {
+    for (uint32_t i = 0; i < count; ++i) {
+        const igxrt_batch_item& it = items[i];
+        igxrt_status st = check_scene(ctx, it.scene);
+        if (st != IGXRT_OK)
+            return st;
+        if (it.mode != IGXRT_MODE_CLOSEST && it.mode != IGXRT_MODE_ANY)
+            return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: unknown mode %u", i, it.mode));
+        if (it.count && (!it.rays || !it.out))
+            return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: rays or out is NULL", i));
+        if (!device_accessible(it.rays) || !device_accessible(it.prev_hit) || !device_accessible(it.out))
+            return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                        format("item %u: an array is not addressable by the device", i));
+    }
+    return IGXRT_OK;
+}
 
 }  // namespace
 
@@ -155,6 +204,14 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
     if (!count || !items)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "autotune needs at least one item");
     const uint32_t reps = opts && opts->reps ? opts->reps : 3;
+    if (opts && (opts->flags & ~IGXRT_TUNE_PLAIN))
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("unknown tune flags 0x%x", opts->flags));
+    const bool plain = opts && (opts->flags & IGXRT_TUNE_PLAIN);
+    if (plain) {
+        igxrt_status st = check_plain_items(ctx, items, count);
+        if (st != IGXRT_OK)
+            return st;
+    }
     uint32_t mask = opts && opts->layouts_mask ? opts->layouts_mask : ((1u << IGXRT_LAYOUT_COUNT) - 1);
     for (uint32_t i = 0; i < count; ++i)  // only layouts every scene has
         for (uint32_t l = 0; l < IGXRT_LAYOUT_COUNT; ++l)
@@ -163,7 +220,8 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
     if (!(mask & ((1u << IGXRT_LAYOUT_COUNT) - 1)))
         return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "autotune: no node layout common to all scenes");
     const std::string key = ctx->device_name + "|" +
-                            ((opts && opts->class_key) ? std::string(opts->class_key) : derive_key(items, count));
+                            ((opts && opts->class_key) ? std::string(opts->class_key) : derive_key(items, count)) +
+                            (plain ? "|plain" : "");
     const char* cache = opts ? opts->cache_path : nullptr;
     if (cache && !(opts && opts->force)) {
         igxrt_launch_params p{};
@@ -181,7 +239,7 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
     DeviceGuard guard(ctx->device);
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");
-    Timer t{ctx, items, count, reps};
+    Timer t{ctx, items, count, reps, plain};
     igxrt_status st = t.init();
     if (st != IGXRT_OK)
         return st;

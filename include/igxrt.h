@@ -462,14 +462,21 @@ igxrt_status igxrt_trace_batch(igxrt_context* ctx, const igxrt_batch_item* items
 /* Autotuner: times candidate launch parameters (node layout, block size,
  * shared stack depth, packet size, refill threshold) on the given items and
  * returns the fastest.  With a cache file, results are stored under
- * (GPU name, class key) and reused without timing. */
+ * (GPU name, class key) and reused without timing.  By default a candidate
+ * is timed as one batched launch over the items (igxrt_trace_batch); with
+ * IGXRT_TUNE_PLAIN it is timed as one plain launch per item, in item order,
+ * on one stream (the igxrt_trace_closest / igxrt_trace_any path), so the
+ * result fits callers that trace the items one call at a time. */
+#define IGXRT_TUNE_PLAIN 1u
+
 typedef struct igxrt_tune_options {
     uint32_t reps;         /* timed repetitions per candidate, 0 = 3 */
     uint32_t layouts_mask; /* bit per IGXRT_LAYOUT_*, 0 = all */
     const char* cache_path;/* NULL = no cache */
     const char* class_key; /* cache key of this workload class, NULL = derived */
     uint32_t force;        /* 1 = ignore a cached entry */
-    uint32_t reserved[3];
+    uint32_t flags;        /* IGXRT_TUNE_PLAIN, or 0 */
+    uint32_t reserved[2];
 } igxrt_tune_options;
 
 igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,

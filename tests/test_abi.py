@@ -70,7 +70,8 @@ def test_python_constants_match_the_header():
         defines[name] = value
     as_int = lambda v: int(v.rstrip("uU"), 0)
     pairs = {"IGXRT_TRACE_HOST_MEMORY": _capi.TRACE_HOST_MEMORY, "IGXRT_TRACE_STAGED": _capi.TRACE_STAGED,
-             "IGXRT_TRACE_INDEPENDENT": _capi.TRACE_INDEPENDENT, "IGXRT_LAYOUT_BVH2": _capi.LAYOUT_BVH2,
+             "IGXRT_TRACE_INDEPENDENT": _capi.TRACE_INDEPENDENT, "IGXRT_TUNE_PLAIN": _capi.TUNE_PLAIN,
+             "IGXRT_LAYOUT_BVH2": _capi.LAYOUT_BVH2,
              "IGXRT_LAYOUT_BVH4": _capi.LAYOUT_BVH4, "IGXRT_LAYOUT_BVH8": _capi.LAYOUT_BVH8,
              "IGXRT_LAYOUT_COUNT": _capi.LAYOUT_COUNT, "IGXRT_MODE_CLOSEST": _capi.MODE_CLOSEST,
              "IGXRT_MODE_ANY": _capi.MODE_ANY, "IGXRT_NO_RAY_HIT": _capi.NO_RAY_HIT}

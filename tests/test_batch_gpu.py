@@ -132,3 +132,31 @@ def test_autotune_and_cache(ctx, tmp_path):
     batch.close()
     with pytest.raises(IgxrtError):
         ctx.autotune([])
+
+
+def test_autotune_plain_launches(ctx, tmp_path):
+    """IGXRT_TUNE_PLAIN times one plain launch per item; its pick traces the
+    items through the plain calls with the same results, and it is cached
+    under its own key."""
+    import torch
+
+    items, plain = _items(ctx, seed=10, nscenes=4, with_empty=False)
+    cache = os.path.join(tmp_path, "tune.txt")
+    p, ms = ctx.autotune(items, reps=2, cache_path=cache, class_key="unit-test", plain=True)
+    assert ms > 0 and p["layout"] in (0, 1, 2) and p["block_size"] in (64, 128, 256)
+    pb, _ = ctx.autotune(items, reps=2, cache_path=cache, class_key="unit-test")
+    lines = open(cache).read().splitlines()
+    assert any("unit-test|plain" in l for l in lines) and any(l.split("\t")[0].endswith("unit-test") for l in lines)
+    before = dict(ctx.launch_params)
+    ctx.set_launch_params(**p)
+    try:
+        for scene, rays, prev, out, mode in items:
+            out.zero_()
+            if mode == 0:
+                ctx.trace_closest(scene, rays, prev, out=out)
+            else:
+                ctx.trace_any(scene, rays, prev, out=out)
+        torch.cuda.synchronize()
+        _check(items, plain)
+    finally:
+        ctx.set_launch_params(**before)

@@ -86,3 +86,50 @@ def test_python_constants_match_the_header():
     assert m and int(m.group(1)) << int(m.group(2)) == _capi.STATIC_SCRATCH_BYTES
     flags = [_capi.TRACE_HOST_MEMORY, _capi.TRACE_STAGED, _capi.TRACE_INDEPENDENT]
     assert all(f & (f - 1) == 0 for f in flags) and len(set(flags)) == 3  # distinct bits
+
+
+# ctypes structures of the Python binding and the C structs they mirror;
+# numpy record layouts and the C records of the same memory image
+_STRUCTS = {"BuildOptions": "igxrt_build_options", "BvhInfo": "igxrt_bvh_info",
+            "LaunchParams": "igxrt_launch_params", "BatchItem": "igxrt_batch_item",
+            "TuneOptions": "igxrt_tune_options", "ServerOptions": "igxrt_server_options",
+            "Request": "igxrt_request", "RequestStats": "igxrt_request_stats",
+            "ServerStats": "igxrt_server_stats", "SceneDesc": "igxrt_scene_desc"}
+_RECORDS = {"TRIANGLE_DTYPE": "igxrt_triangle", "RAY_DTYPE": "igxrt_ray", "HIT_DTYPE": "igxrt_hit",
+            "PRIM_RECORD_DTYPE": "igxrt_prim_record", "BVH2_NODE_DTYPE": "igxrt_bvh2_node",
+            "BVH4_NODE_DTYPE": "igxrt_bvh4_node", "BVH8_NODE_DTYPE": "igxrt_bvh8_node",
+            "CAMERA_DTYPE": "igxrt_camera", "CUBE_DTYPE": "igxrt_cube"}
+
+
+def test_binding_layouts_match_the_header(tmp_path):
+    """Every ctypes structure has the size and field offsets of its C struct
+    (compiled against include/igxrt.h by the host compiler), and every numpy
+    record layout the size of its C record."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "igxrt.h"', "int main(void) {"]
+    expect = []
+    for py, c in _STRUCTS.items():
+        cls = getattr(_capi, py)
+        lines.append(f'    printf("%zu\\n", sizeof({c}));')
+        expect.append((f"sizeof {c}", ctypes.sizeof(cls)))
+        for name, *_ in cls._fields_:
+            lines.append(f'    printf("%zu\\n", offsetof({c}, {name}));')
+            expect.append((f"{c}.{name}", getattr(cls, name).offset))
+    for py, c in _RECORDS.items():
+        lines.append(f'    printf("%zu\\n", sizeof({c}));')
+        expect.append((f"sizeof {c}", getattr(_capi, py).itemsize))
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layouts.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layouts"
+    subprocess.run([cc, "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert len(got) == len(expect)
+    wrong = [(what, want, g) for (what, want), g in zip(expect, got) if want != g]
+    assert not wrong, wrong

@@ -133,3 +133,27 @@ def test_binding_layouts_match_the_header(tmp_path):
     assert len(got) == len(expect)
     wrong = [(what, want, g) for (what, want), g in zip(expect, got) if want != g]
     assert not wrong, wrong
+
+
+def test_integration_cpp_example_compiles_and_links(engine_lib, tmp_path):
+    """The C++ example of INTEGRATION.md, inside a function that declares its
+    inputs, compiles against include/igxrt.h and links against libigxrt.so."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    block = re.search(r"```cpp\n(.*?)```", doc, flags=re.S).group(1)
+    body = "\n".join(l for l in block.splitlines() if not l.startswith("#include"))
+    src = tmp_path / "example.cpp"
+    src.write_text("#include <cstdio>\n#include <vector>\n#include \"igxrt.h\"\n"
+                   "void example(const std::vector<igxrt_triangle>& triangles, const igxrt_ray* d_rays,\n"
+                   "             igxrt_hit* d_hits, uint32_t w, uint32_t h, void* stream,\n"
+                   "             const igxrt_ray* h_rays, igxrt_hit* h_hits, uint32_t n) {\n"
+                   + body + "\n}\nint main() { return 0; }\n")
+    lib_dir = os.path.dirname(_capi.LIB_PATH)
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", os.path.dirname(HEADER), str(src),
+                    "-o", str(tmp_path / "example"), "-L", lib_dir, "-ligxrt", "-Wl,-rpath," + lib_dir],
+                   check=True)

@@ -511,6 +511,7 @@ igxrt_status igxrt_scene_destroy(igxrt_scene* scene) {
         DeviceGuard guard(scene->device);
         cudaDeviceSynchronize();
         cudaFree(scene->d_mem);
+        cudaFree(scene->refit_boxes);
     }
     delete scene;
     return IGXRT_OK;

@@ -58,6 +58,10 @@ struct igxrt_scene {
     uint32_t* refit_words = nullptr;
     // BVH8 slots' sources in the BVH2 layout (8 per BVH8 node), for the refit
     const uint32_t* src8 = nullptr;
+    // GPU refit scratch, two float4 per record ({box lo, leaf_end}, {box hi,
+    // 0}), written by the record pass and read by the node climb; allocated
+    // at the scene's first GPU refit, freed with the scene
+    float4* refit_boxes = nullptr;
 
     // A layout can be traced when the tree has it; an empty scene has none
     // and traces as all misses in every layout.

@@ -9,9 +9,13 @@
 //      state word; a non-finite coordinate records the object and turns the
 //      later passes into no-ops, so a rejected refit leaves the scene as it was;
 //   2. records: primitive records (triangle p0/e1/e2, sphere centre/radius, cube
-//      corners) and the scene's triangle and plane copies are rewritten;
+//      corners) and the scene's triangle and plane copies are rewritten, and
+//      every record's object box is stored in leaf order beside its leaf_end
+//      flag (the scene's refit scratch);
 //   3. nodes: a thread per node whose children are all leaves writes that
-//      node's slot boxes, then climbs through the parent links.  At each parent
+//      node's slot boxes (a leaf slot from the stored boxes: one contiguous
+//      read per record, shared by the BVH2 and BVH4 climbs), then climbs
+//      through the parent links.  At each parent
 //      an atomic arrival counter lets only the thread of the last interior child
 //      go on, so every node is written once, after all of its children.  Nothing
 //      waits on another thread: a thread either continues or exits;
@@ -122,6 +126,7 @@ struct RefitArgs {
     igxrt_bvh8_node* nodes8;
     const uint32_t* src8;
     uint32_t n8;
+    float4* boxes;  // per record, in leaf order: {lo, leaf_end}, {hi, 0}
 };
 
 static_assert(kRefitStateWords == 8, "refit state words");
@@ -165,6 +170,9 @@ __global__ void refit_records_kernel(RefitArgs a) {
         rec[3 * (size_t)i] = r0;
         rec[3 * (size_t)i + 1] = r1;
         rec[3 * (size_t)i + 2] = r2;
+        const Box ob = object_box<false>(o, id);
+        a.boxes[2 * (size_t)i] = make_float4(ob.lo[0], ob.lo[1], ob.lo[2], r1.w);  // r1.w: leaf_end
+        a.boxes[2 * (size_t)i + 1] = make_float4(ob.hi[0], ob.hi[1], ob.hi[2], 0.f);
     }
     if (tris16) {
         const float4* src = reinterpret_cast<const float4*>(o.tris);
@@ -179,12 +187,18 @@ __global__ void refit_records_kernel(RefitArgs a) {
         a.scene_planes[i] = o.planes[i];
 }
 
+// Padded box of the leaf whose records start at ~ref: the union, in record
+// order, of the object boxes the record pass stored.
 __device__ Box leaf_box(const RefitArgs& a, int32_t ref, float pad) {
     Box b;
     b.reset();
     for (uint32_t i = (uint32_t)~ref;; ++i) {
-        b.grow(object_box<false>(a.obj, a.prims[i].prim));
-        if (a.prims[i].leaf_end)
+        const float4 l = __ldg(a.boxes + 2 * (size_t)i), h = __ldg(a.boxes + 2 * (size_t)i + 1);
+        Box ob;
+        ob.lo[0] = l.x, ob.lo[1] = l.y, ob.lo[2] = l.z;
+        ob.hi[0] = h.x, ob.hi[1] = h.y, ob.hi[2] = h.z;
+        b.grow(ob);
+        if (__float_as_uint(l.w))
             break;
     }
     b.pad(pad);
@@ -378,6 +392,14 @@ igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igx
     a.n8 = scene->node_count[IGXRT_LAYOUT_BVH8];
 
     const uint32_t n = a.obj.count();
+    if (n && !scene->refit_boxes) {  // once per scene, at its first refit
+        const cudaError_t e = cudaMalloc(&scene->refit_boxes, 2 * sizeof(float4) * (size_t)n);
+        if (e != cudaSuccess) {
+            scene->refit_boxes = nullptr;
+            return cuda_fail(ctx, e, "refit scratch allocation");
+        }
+    }
+    a.boxes = scene->refit_boxes;
     const size_t words = kRefitStateWords + (size_t)a.n2 + a.n4;
     cudaError_t e = cudaMemsetAsync(a.state, 0, words * sizeof(uint32_t), s);
     if (e != cudaSuccess)

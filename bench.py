@@ -1140,11 +1140,13 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
     reference re-uploads moving geometry per frame, niels_scene.cpp:61-70).
     A step is one frame: new positions (device-resident) -> igxrt_scene_refit
     -> 1080p primaries.  Beside it: the same frame with a full GPU rebuild
-    (igxrt_scene_create_gpu) instead of the refit."""
+    (igxrt_scene_create_gpu) instead of the refit.  e2e: the positions come
+    from pinned host memory every frame and the hits go back to it."""
     import torch
 
     import igx_raytracing_gb300 as igx
     from igx_raytracing_gb300 import BVH, scenes
+    from igx_raytracing_gb300.dist import max_over_ranks
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
@@ -1193,6 +1195,31 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
     trace_only = statistics.mean(_event_ms(torch, lambda: ctx.trace_closest(scene, d_rays, out=out),
                                            args.steps, flush, stream))
     rebuild_ms = statistics.mean(_event_ms(torch, rebuild_frame, args.steps, flush, stream))
+    # end to end: each frame's positions come from pinned host memory (the
+    # refit copies them up with IGXRT_TRACE_HOST_MEMORY) and its hits go to
+    # pinned host memory in place; the frame's camera rays stay resident
+    host_frames = [f.cpu().pin_memory() for f in frames]
+    host_out = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory()
+
+    def e2e_frame():
+        f = host_frames[counter["k"] % len(frames)]
+        counter["k"] += 1
+        scene.refit(f.numpy().view(igx.TRIANGLE_DTYPE).reshape(-1))
+        ctx.trace_closest(scene, d_rays, out=host_out)
+        stream.synchronize()
+
+    for _ in range(args.warmup):
+        e2e_frame()
+    e2e_s = []
+    for _ in range(args.steps):
+        flush.fill_(0.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_frame()
+        e2e_s.append(time.perf_counter() - t0)
+    e2e_ms = max_over_ranks(1000 * statistics.mean(e2e_s), dev)
+    e2e_spread = (round(1000 * min(e2e_s), 3), round(1000 * max(e2e_s), 3))
+
     nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
     n = len(rays)
     b = algorithmic_bytes(nf, pf, 0, False, layout)
@@ -1211,9 +1238,13 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
                         "gpu_rebuild_plus_trace_ms": round(rebuild_ms, 4),
                         "frames_per_s_refit": round(1e3 / ms, 1),
                         "frames_per_s_gpu_rebuild": round(1e3 / rebuild_ms, 1)},
-                 e2e={"value": round(world * n / (ms / 1e3) / 1e6, 3), "unit": UNIT,
-                      "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0, "ms_per_step": round(ms, 4),
-                      "note": "positions and rays resident: a frame's geometry arrives from a device kernel"},
+                 e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
+                      "h2d_bytes_per_step": int(host_frames[0].numel() * 4),
+                      "d2h_bytes_per_step": int(host_out.numel() * 4), "ms_per_step": round(e2e_ms, 4),
+                      "ms_min_max": e2e_spread, "frames_per_s": round(1e3 / e2e_ms, 1),
+                      "route": "positions from pinned host memory through igxrt_scene_refit "
+                               "(IGXRT_TRACE_HOST_MEMORY: copied up, then refit), hits written in place "
+                               "to pinned host memory; camera rays resident; one synchronization per frame"},
                  gpu_launches=args.steps * refit_launches, clocks=clk)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -174,7 +174,10 @@ class ClockSampler:
         self.device = device
         self.interval_ms = interval_ms
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", f"clocks_dev{device}.csv")
+        # the raw samples: IGXRT_CLOCKS_DIR if set, else the temp directory
+        import tempfile
+        self.path = os.path.join(os.environ.get("IGXRT_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 f"igxrt_clocks_dev{device}.csv")
 
     def start(self):
         """Starts sampling and returns once the first sample is in, so even a

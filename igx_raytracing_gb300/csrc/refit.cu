@@ -272,8 +272,9 @@ __global__ void refit_nodes_kernel(RefitArgs a) {
 // slots, eight lanes per node, one per slot.  The node's bounds are reduced
 // across the eight lanes with the lower slot as the first operand of every
 // comparison, which picks the same element as the host's slot-order loop in
-// bvh8_quantize_node (ties, signed zeros included); each lane then quantizes
-// its own slot with the same bvh8_exponent / bvh8_quantize, and the bytes are
+// bvh8_quantize_node (ties, signed zeros included); three lanes find the
+// axes' exponents with the same bvh8_exponent, each lane quantizes its own
+// slot with the same bvh8_quantize, and the bytes are
 // packed into words with shuffles and stored as four 16-byte words.
 __global__ void __launch_bounds__(128) refit_bvh8_kernel(RefitArgs a) {
     if (a.state[kWordBad])
@@ -308,13 +309,20 @@ __global__ void __launch_bounds__(128) refit_bvh8_kernel(RefitArgs a) {
             nlo[k] = olo < nlo[k] ? olo : nlo[k];
             nhi[k] = nhi[k] < ohi ? ohi : nhi[k];
         }
-    uint32_t word[6];  // lo_x, hi_x, lo_y, hi_y, lo_z, hi_z: this lane's byte in place
-    int e[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         nlo[k] = __shfl_sync(0xffffffffu, nlo[k], 0, 8);
         nhi[k] = __shfl_sync(0xffffffffu, nhi[k], 0, 8);
-        e[k] = live ? bvh8_exponent(nlo[k], nhi[k]) : 0;
+    }
+    // lanes 0, 1 and 2 of the node find the exponent of axis x, y and z
+    const float alo = slot == 0 ? nlo[0] : (slot == 1 ? nlo[1] : nlo[2]);
+    const float ahi = slot == 0 ? nhi[0] : (slot == 1 ? nhi[1] : nhi[2]);
+    const int my_e = live && slot < 3 ? bvh8_exponent(alo, ahi) : 0;
+    uint32_t word[6];  // lo_x, hi_x, lo_y, hi_y, lo_z, hi_z: this lane's byte in place
+    int e[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e[k] = __shfl_sync(0xffffffffu, my_e, k, 8);
         uint8_t ql = 0, qh = 0;
         if (used)
             bvh8_quantize(nlo[k], e[k], lo[k], hi[k], ql, qh);

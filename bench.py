@@ -36,13 +36,25 @@ route passes the pinned arrays to the stream-ordered calls: the kernels read
 the rays and write the results in host memory over NVLink-C2C, with one
 synchronization per step.  Beside it: host-memory calls on the same memory
 (each returns with its results in host memory), and those calls staged
-(copy up, trace, copy down).  --impl reference times the CPU transcription
-of the reference's traversal (the oracle's BVH traversal over the same BVH)
-on all host cores.
+(copy up, trace, copy down).
+
+The default (sphere) line also carries, measured in the same run with their
+own clock records: `incoherent1m` (the roofline target's workload),
+`incoherent` (2M triangles), `batch` (64 scenes: one batched launch against
+64 plain launches) and `serve` (--serve-seconds of Poisson arrivals at
+--rate, latency from each request's scheduled arrival).  --no-extras leaves
+them out.
+
+--impl reference times the reference's traversal restated on the CPU (the
+oracle's BVH traversal, on a BVH the oracle builds itself) on all host cores,
+every ray of the same workload each step; the engine library is not loaded.
+--gpus N starts N ranks (one per GPU) when not already under torchrun; each
+rank traces the whole step on its own GPU (weak scaling).
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -75,33 +87,53 @@ def log(*a):
 # Workloads: a list of batches (rays, prev, mode) over one triangle set
 # --------------------------------------------------------------------------
 
-def make_workload(name: str, ctx=None):
+L2_NOTE = "GPU arm: a 256 MiB buffer is written between timed steps; inputs stay resident"
+
+
+def workload_config(name: str, tris, batches) -> dict:
+    """The workload's description, identical in the engine and reference
+    arms: its name, sizes and a digest of every ray, prev_hit and query mode
+    of a step (both arms trace the same bytes)."""
+    h = hashlib.sha1()
+    for _, rays, prev, mode in batches:
+        h.update(np.ascontiguousarray(rays).tobytes())
+        if prev is not None:
+            h.update(np.ascontiguousarray(prev).tobytes())
+        h.update(bytes([mode]))
+    return {"workload": name, "triangles": int(len(tris)),
+            "rays_per_step": int(sum(len(b[1]) for b in batches)), "rays_sha1": h.hexdigest()[:16],
+            "l2": L2_NOTE}
+
+
+WORKLOAD_NAMES = {"small": "heightfield_4k_256x256_primary",
+                  "incoherent": "random_2m_tris_4m_incoherent_rays",
+                  "incoherent1m": "random_1m_tris_4m_incoherent_rays",
+                  "sphere": "sphere_1m_1080p_primary_bounce_shadow"}
+
+
+def make_workload(name: str, primary_hits=None):
+    """(triangles, batches, config) of a workload.  The sphere's bounce and
+    shadow rays start at the primary hits: `primary_hits(tris, rays)` gives
+    them (the engine in the engine arm, the oracle in the reference arm; the
+    two are equal bit for bit, which the CPU-baseline leg checks)."""
     from igx_raytracing_gb300 import scenes
 
     if name == "small":
         tris, rays = scenes.workload_small()
-        return tris, [("primary", rays, None, 0)], {"workload": "heightfield_4k_256x256_primary",
-                                                    "triangles": len(tris)}
-    if name in ("incoherent", "incoherent1m"):
+        batches = [("primary", rays, None, 0)]
+    elif name in ("incoherent", "incoherent1m"):
         nt = 2_097_152 if name == "incoherent" else 1_048_576
         tris, rays = scenes.workload_incoherent(nt, 4_194_304, variant=0 if name == "incoherent" else 1)
-        return tris, [("incoherent", rays, None, 0)], {
-            "workload": f"random_{nt // 1048576 if nt >= 1048576 else nt}m_tris_4m_incoherent_rays",
-            "triangles": nt}
-    if name == "sphere":
+        batches = [("incoherent", rays, None, 0)]
+    elif name == "sphere":
         tris, prim = scenes.workload_sphere_primary()
-        # secondaries start at the primary hits found by the engine (the
-        # parity tests check those hits against the oracle)
-        assert ctx is not None
-        scene = ctx.create_scene(tris)
-        hits = scene.trace_geometry(prim)
-        scene.close()
+        hits = primary_hits(tris, prim)
         bounce, shadow, prev = scenes.secondary_rays(tris, prim, hits, scenes.SPHERE_LIGHT,
                                                      scenes.seed_for(2, 50))
-        return tris, [("primary", prim, None, 0), ("bounce", bounce, prev, 0),
-                      ("shadow", shadow, prev, 1)], {
-            "workload": "sphere_1m_1080p_primary_bounce_shadow", "triangles": len(tris)}
-    raise SystemExit(f"unknown workload {name}")
+        batches = [("primary", prim, None, 0), ("bounce", bounce, prev, 0), ("shadow", shadow, prev, 1)]
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return tris, batches, workload_config(WORKLOAD_NAMES[name], tris, batches)
 
 
 def algorithmic_bytes(nf: np.ndarray, pf: np.ndarray, mode: int, has_prev: bool, layout: int) -> int:
@@ -167,7 +199,7 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int, interval_ms: int = 20):
+    def __init__(self, device: int, interval_ms: int = 20, tag: str = ""):
         """interval_ms: 20 covers timed regions of a few ms; a long serving
         run samples every 250 ms, since each nvidia-smi query briefly holds
         driver locks that the serving thread's CUDA calls then wait on."""
@@ -177,7 +209,7 @@ class ClockSampler:
         # the raw samples: IGXRT_CLOCKS_DIR if set, else the temp directory
         import tempfile
         self.path = os.path.join(os.environ.get("IGXRT_CLOCKS_DIR") or tempfile.gettempdir(),
-                                 f"igxrt_clocks_dev{device}.csv")
+                                 f"igxrt_clocks_dev{device}{tag}.csv")
 
     def start(self):
         """Starts sampling and returns once the first sample is in, so even a
@@ -230,7 +262,7 @@ class ClockSampler:
 # triangle test) on all host cores, over a bounded strided sample
 # --------------------------------------------------------------------------
 
-def cpu_baseline(bvh, batches, budget_s: float = 12.0, layout: int = 0) -> dict:
+def cpu_baseline(bvh, batches, budget_s: float = 12.0, layout: int = 0, engine_primary_hits=None) -> dict:
     from oracle import pyoracle
 
     nodes, prims = bvh.arrays(layout)
@@ -264,10 +296,18 @@ def cpu_baseline(bvh, batches, budget_s: float = 12.0, layout: int = 0) -> dict:
         if stride > 1:
             break
     what = "the whole workload" if stride == 1 else f"every {stride}th ray of each batch"
-    return {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{passes} pass(es) over {what} ({n} rays, {dt:.1f} s): the oracle's BVH "
-                      "traversal over the engine's BVH2 with the triangle test transcribed from "
-                      "primitive.glsl:239-284"}
+    out = {"value": round(n / dt / 1e6, 4), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{passes} pass(es) over {what} ({n} rays, {dt:.1f} s): the oracle's BVH "
+                     "traversal over the engine's BVH2 with the triangle test transcribed from "
+                     "primitive.glsl:239-284"}
+    if engine_primary_hits is not None:
+        # the engine's primary hits (the origins of the step's secondary rays)
+        # against the oracle's traversal, every ray
+        _, rays, prev, _ = batches[0]
+        expect = pyoracle.bvh_trace(layout, nodes, prims, rays, prev, mode=0, threads=threads)
+        out["primary_hits_equal_oracle"] = bool(
+            np.ascontiguousarray(engine_primary_hits).tobytes() == expect.tobytes())
+    return out
 
 
 def linear_loop_rate(tris, batches, max_rays: int = 256) -> float:
@@ -281,59 +321,59 @@ def linear_loop_rate(tris, batches, max_rays: int = 256) -> float:
 
 
 # --------------------------------------------------------------------------
-# Reference arm
+# Reference arm: the reference's traversal restated on the CPU (the oracle),
+# over a BVH the oracle builds itself; the engine library is never loaded
 # --------------------------------------------------------------------------
 
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
-    from igx_raytracing_gb300 import BVH, scenes
     from oracle import pyoracle
 
+    if args.workload not in WORKLOAD_NAMES:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"the CPU reference arm covers {sorted(WORKLOAD_NAMES)}, not {args.workload}"}))
+        return
     pyoracle.lib()
-    if args.workload == "sphere":
-        # primary hits come from the oracle's own traversal here (no GPU use)
-        tris, prim = scenes.workload_sphere_primary()
-        bvh = BVH.build(tris)
-        nodes, prims = bvh.arrays(0)
-        hits = pyoracle.bvh_trace(0, nodes, prims, prim)
-        bounce, shadow, prev = scenes.secondary_rays(tris, prim, hits, scenes.SPHERE_LIGHT,
-                                                     scenes.seed_for(2, 50))
-        batches = [("primary", prim, None, 0), ("bounce", bounce, prev, 0), ("shadow", shadow, prev, 1)]
-        cfg = {"workload": "sphere_1m_1080p_primary_bounce_shadow", "triangles": len(tris)}
-    else:
-        tris, batches, cfg = make_workload(args.workload)
-        bvh = BVH.build(tris)
     threads = pyoracle.hardware_threads()
-    nodes, prims = bvh.arrays(0)
+    trees = {}
+
+    def oracle_tree(tris):
+        if "nodes" not in trees:
+            t0 = time.perf_counter()
+            trees["nodes"], trees["prims"] = pyoracle.bvh_build(tris)
+            trees["build_s"] = time.perf_counter() - t0
+        return trees["nodes"], trees["prims"]
+
+    def primary_hits(tris, rays):
+        nodes, prims = oracle_tree(tris)
+        return pyoracle.bvh_trace(0, nodes, prims, rays, threads=threads)
+
+    tris, batches, cfg = make_workload(args.workload, primary_hits)
+    nodes, prims = oracle_tree(tris)
     total = sum(len(b[1]) for b in batches)
-    stride = max(1, total // 1000000)  # about a million rays per step
     times = []
-    nrays = 0
     for step in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        n = 0
         for _, rays, prev, mode in batches:
-            off = step % stride
-            r = rays[off::stride]
-            p = None if prev is None else prev[off::stride]
-            pyoracle.bvh_trace(0, nodes, prims, r, p, mode=mode, threads=threads)
-            n += len(r)
+            pyoracle.bvh_trace(0, nodes, prims, rays, prev, mode=mode, threads=threads)
         dt = time.perf_counter() - t0
         if step >= args.warmup:
             times.append(dt)
-            nrays += n
-    value = nrays / sum(times) / 1e6
+    value = args.steps * total / sum(times) / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * statistics.mean(times), 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(cfg, rays_per_step=total, sample_stride=stride),
-            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
-                             "kind": "port",
-                             "sample": f"each step traces every {stride}th ray of the workload "
-                                       "with the oracle's BVH traversal (a transcription of "
-                                       "primitive.glsl:239-284 / trace.glsl:9-98) on all cores"},
+            "config": cfg,
+            "setup": {"bvh": "the oracle's own binned-SAH BVH2 (oracle/bvh_build_oracle.c)",
+                      "bvh_nodes": int(len(nodes)), "bvh_build_s": round(trees["build_s"], 2),
+                      "secondaries_from": "the oracle's own primary hits" if args.workload == "sphere" else None},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"every ray of the workload ({total} per step) each step, traced by "
+                                       "the oracle's BVH traversal (the triangle test of "
+                                       "primitive.glsl:239-284 in trace.glsl:9-98's closest / any-hit "
+                                       "rules) on all host cores"},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -343,21 +383,27 @@ def run_reference(args, rank: int, world: int):
 # Engine arm
 # --------------------------------------------------------------------------
 
-def run_engine(args, rank: int, world: int, local_rank: int):
+def measure_plain(args, ctx, dev, name: str, world: int, lite: bool = False) -> dict:
+    """One workload through the plain trace calls: the step (every batch one
+    launch, in order) timed with CUDA events, the per-launch figures and the
+    roofline of the dominant launch, e2e with pinned host buffers; unless
+    `lite`, also the host-memory and staged e2e routes, the batched form of
+    the step, and the CPU baseline."""
     import torch
 
     import igx_raytracing_gb300 as igx
     from igx_raytracing_gb300 import BVH
     from igx_raytracing_gb300.dist import max_over_ranks
 
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    ctx = igx.Context(local_rank)
-    if args.layout is not None:
-        ctx.set_launch_params(layout=args.layout)
-    layout = ctx.launch_params["layout"]
+    def engine_primary_hits(tris, rays):
+        scene = ctx.create_scene(tris)
+        hits = scene.trace_geometry(rays)
+        scene.close()
+        engine_primary_hits.hits = hits
+        return hits
 
-    tris, batches, cfg = make_workload(args.workload, ctx)
+    engine_primary_hits.hits = None
+    tris, batches, cfg = make_workload(name, engine_primary_hits)
     t0 = time.perf_counter()
     bvh = BVH.build(tris)
     build_s = time.perf_counter() - t0
@@ -366,12 +412,12 @@ def run_engine(args, rank: int, world: int, local_rank: int):
 
     # device-resident inputs and outputs
     dev_batches = []
-    for name, rays, prev, mode in batches:
+    for bname, rays, prev, mode in batches:
         d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
         d_prev = None if prev is None else torch.from_numpy(prev.view(np.int32).copy()).to(dev)
         out = (torch.empty((len(rays), 4), dtype=torch.float32, device=dev) if mode == 0
                else torch.empty(len(rays), dtype=torch.int32, device=dev))
-        dev_batches.append((name, d_rays, d_prev, mode, out))
+        dev_batches.append((bname, d_rays, d_prev, mode, out))
     total_rays = sum(len(b[1]) for b in batches)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
@@ -380,12 +426,15 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     # layout is forced); the plain launches below then run with it
     items = [(scene, d_rays, d_prev, out, mode) for _, d_rays, d_prev, mode, out in dev_batches]
     tuned = tuned_batch = None
+    saved_params = ctx.launch_params
+    tune_s = 0.0
     if args.layout is None and not args.no_tune:
         t0 = time.perf_counter()
         # the plain launches as the step issues them (one per batch, in order)
         tuned, _ = ctx.autotune(items, reps=5, force=True, plain=True)
         # and, for the batched figure, the shape of one launch over all batches
-        tuned_batch, _ = ctx.autotune(items, reps=3, force=True) if len(items) > 1 else (None, 0.0)
+        if len(items) > 1 and not lite:
+            tuned_batch, _ = ctx.autotune(items, reps=3, force=True)
         tune_s = time.perf_counter() - t0
         ctx.set_launch_params(**tuned)
     layout = ctx.launch_params["layout"]
@@ -393,10 +442,10 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     # The shadow rays and their prev_hit come from the primary hits, not from
     # the bounce launch queued before them: that launch is flagged
     # IGXRT_TRACE_INDEPENDENT and may start while the bounce launch drains.
-    indep = [i > 0 and name == "shadow" for i, (name, *_rest) in enumerate(dev_batches)]
+    indep = [i > 0 and bname == "shadow" for i, (bname, *_rest) in enumerate(dev_batches)]
 
     def step(events=None, overlap=True):
-        for i, (name, d_rays, d_prev, mode, out) in enumerate(dev_batches):
+        for i, (bname, d_rays, d_prev, mode, out) in enumerate(dev_batches):
             if events is not None:
                 events[i][0].record(stream)
             f = ctx.trace_closest if mode == 0 else ctx.trace_any
@@ -414,7 +463,7 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     # the timed steps: events at step boundaries only (an event between two
     # launches would keep the second from starting early)
     sev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
-    clocks = ClockSampler(local_rank)
+    clocks = ClockSampler(dev.index or 0, tag=f"_{name}")
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -454,7 +503,7 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     # the same step through the batched engine: all batches in one persistent,
     # graph-captured launch (its own tuned shape), for the batched-vs-plain figure
     batched = None
-    if len(dev_batches) > 1:
+    if len(dev_batches) > 1 and not lite:
         batch = ctx.create_batch(items, params=tuned_batch or ctx.launch_params)
         for _ in range(args.warmup):
             batch.launch()
@@ -472,15 +521,17 @@ def run_engine(args, rank: int, world: int, local_rank: int):
         bms = max_over_ranks(statistics.mean(bts), dev)
         batched = {"ms_per_step": round(bms, 4), "mrays_s": round(world * total_rays / (bms / 1e3) / 1e6, 3),
                    "over_plain": round(step_ms / bms, 3), "launches_per_step": 1}
+        if tuned_batch:
+            batched["launch"] = tuned_batch
 
     # roofline: algorithmic bytes per launch from the instrumented kernel
     peaks = measured_peaks()
     per_batch = []
-    for i, (name, rays, prev, mode) in enumerate(batches):
+    for i, (bname, rays, prev, mode) in enumerate(batches):
         nf, pf = ctx.count_fetches(scene, rays, prev, mode=mode, layout=layout)
         b = algorithmic_bytes(nf, pf, mode, prev is not None, layout)
         ms = float(launch_ms[:, i].mean())
-        per_batch.append({"batch": name, "rays": len(rays), "mode": "any" if mode else "closest",
+        per_batch.append({"batch": bname, "rays": len(rays), "mode": "any" if mode else "closest",
                           "ms": round(ms, 4), "bytes": b, "nodes_per_ray": round(float(nf.mean()), 3),
                           "prims_per_ray": round(float(pf.mean()), 3),
                           "gbs": round(b / (ms / 1e3) / 1e9, 1),
@@ -491,13 +542,13 @@ def run_engine(args, rank: int, world: int, local_rank: int):
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
                 "traffic": traffic_from_profiles(cfg["workload"], dom["batch"], layout),
                 "kernel": f"trace_kernel<{LAYOUT_NAMES[layout]},{dom['mode']}> ({dom['batch']})",
-                "peak_source": peaks["source"]}
+                "peak_source": peaks["source"], "bytes_per_launch": dom["bytes"]}
     step_bytes = sum(b["bytes"] for b in per_batch)
 
     # e2e: the same rays through the C ABI from pinned host buffers
     host = []
     h2d = d2h = 0
-    for i, (name, rays, prev, mode) in enumerate(batches):
+    for i, (bname, rays, prev, mode) in enumerate(batches):
         hr = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).pin_memory()
         hp = torch.from_numpy(prev.view(np.int32).copy()).pin_memory() if prev is not None else None
         ho = (torch.empty((len(rays), 4), dtype=torch.float32) if mode == 0
@@ -526,6 +577,8 @@ def run_engine(args, rank: int, world: int, local_rank: int):
             else:
                 ctx.trace_any(scene, r, pv, out=ho.numpy().view(np.uint32))
 
+    spread = []  # (fastest, slowest) step of each route, ms
+
     def e2e_ms_per_step(step_fn):
         for _ in range(args.warmup):
             step_fn()
@@ -539,99 +592,132 @@ def run_engine(args, rank: int, world: int, local_rank: int):
         spread.append((round(1000 * min(times), 3), round(1000 * max(times), 3)))
         return max_over_ranks(1000 * statistics.mean(times), dev)
 
-    spread = []  # (fastest, slowest) step of each route, ms
-    e2e_ms = e2e_ms_per_step(e2e_async_step)
-    host_call_ms = e2e_ms_per_step(e2e_host_call_step)
-    ctx.stage_host_arrays = True  # IGXRT_TRACE_STAGED: copy up, trace, copy down
-    staged_ms = e2e_ms_per_step(e2e_host_call_step)
-    ctx.stage_host_arrays = False
-    e2e_value = world * total_rays / (e2e_ms / 1e3) / 1e6
     mrays = lambda ms: round(world * total_rays / (ms / 1e3) / 1e6, 3)
+    e2e_ms = e2e_ms_per_step(e2e_async_step)
+    e2e = {"value": mrays(e2e_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3), "ms_min_max": spread[0],
+           "route": "pinned host tensors through the stream-ordered calls: the kernels read "
+                    "the rays and write the results in host memory over NVLink-C2C; one "
+                    "synchronization per step"}
+    if not lite:
+        host_call_ms = e2e_ms_per_step(e2e_host_call_step)
+        ctx.stage_host_arrays = True  # IGXRT_TRACE_STAGED: copy up, trace, copy down
+        staged_ms = e2e_ms_per_step(e2e_host_call_step)
+        ctx.stage_host_arrays = False
+        e2e["host_calls"] = {"value": mrays(host_call_ms), "ms_per_step": round(host_call_ms, 3),
+                             "ms_min_max": spread[1],
+                             "route": "IGXRT_TRACE_HOST_MEMORY calls on the same pinned memory, "
+                                      "each returning with its results in host memory"}
+        e2e["staged"] = {"value": mrays(staged_ms), "ms_per_step": round(staged_ms, 3),
+                         "ms_min_max": spread[2],
+                         "route": "IGXRT_TRACE_STAGED: copy up, trace, copy down, per call"}
 
-    if rank != 0:
-        return
+    setup = {"layout": LAYOUT_NAMES[layout], "launch": ctx.launch_params, "bvh_build_s": round(build_s, 2),
+             "bvh2_nodes": info["bvh2_nodes"], "sah_cost": round(info["sah_cost"], 2),
+             "parallelism": (f"replicas x{world}: every rank traces the whole step on its own GPU "
+                             "(weak scaling)") if world > 1 else "single gpu"}
+    if tuned is not None:
+        setup["launch_chosen_by"] = f"igxrt_autotune with IGXRT_TUNE_PLAIN on the step's batches ({tune_s:.1f} s)"
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": dict(cfg, rays_per_step=total_rays, layout=LAYOUT_NAMES[layout],
-                           launch=ctx.launch_params, bvh_build_s=round(build_s, 2),
-                           bvh2_nodes=info["bvh2_nodes"], sah_cost=round(info["sah_cost"], 2),
-                           l2="256 MiB buffer written between timed steps",
-                           parallelism=f"replicas x{world}" if world > 1 else "single gpu"),
-            "roofline": roofline,
+            "data": "synthetic", "config": cfg, "setup": setup, "roofline": roofline,
             "roofline_step": {"bytes": step_bytes, "achieved": round(step_bytes / (step_ms / 1e3) / 1e9, 1),
                               "unit": "GB/s", "frac": round(step_bytes / (step_ms / 1e3) / 1e9 / peaks["hbm_gbs"], 4)},
-            **({"launches": {"independent": [b[0] for b, f in zip(dev_batches, indep) if f],
-                             "sum_of_launches_alone_ms": round(serial_step_ms, 4),
-                             "what": "shadow launch queued with IGXRT_TRACE_INDEPENDENT after the bounce "
-                                     "launch (both read the primary hits only); value times whole steps"}}
-               if any(indep) else {}),
-            "batches": per_batch,
-            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_ms, 3),
-                    "ms_min_max": spread[0],
-                    "route": "pinned host tensors through the stream-ordered calls: the kernels read "
-                             "the rays and write the results in host memory over NVLink-C2C; one "
-                             "synchronization per step",
-                    "host_calls": {"value": mrays(host_call_ms), "ms_per_step": round(host_call_ms, 3),
-                                   "ms_min_max": spread[1],
-                                   "route": "IGXRT_TRACE_HOST_MEMORY calls on the same pinned memory, "
-                                            "each returning with its results in host memory"},
-                    "staged": {"value": mrays(staged_ms), "ms_per_step": round(staged_ms, 3),
-                               "ms_min_max": spread[2],
-                               "route": "IGXRT_TRACE_STAGED: copy up, trace, copy down, per call"}},
-            "gpu_launches": args.steps * nb,
-            "clocks": clk,
+            "batches": per_batch, "e2e": e2e, "gpu_launches": args.steps * nb, "clocks": clk,
             "wall_s_timed_region": round(wall, 3)}
-    if tuned is not None:
-        line["config"]["launch_chosen_by"] = (f"igxrt_autotune with IGXRT_TUNE_PLAIN on the step's batches "
-                                              f"({tune_s:.1f} s with the batched tuning)")
+    if any(indep):
+        line["launches"] = {"independent": [b[0] for b, f in zip(dev_batches, indep) if f],
+                            "sum_of_launches_alone_ms": round(serial_step_ms, 4),
+                            "what": "shadow launch queued with IGXRT_TRACE_INDEPENDENT after the bounce "
+                                    "launch (both read the primary hits only); value times whole steps"}
     if batched is not None:
-        if tuned_batch:
-            batched["launch"] = tuned_batch
         line["batched"] = batched
-    if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(bvh, batches, layout=0)
+    if not lite and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(bvh, batches, layout=0, engine_primary_hits=engine_primary_hits.hits)
         line["cpu_baseline"]["linear_loop_mrays_s"] = round(linear_loop_rate(tris, batches), 6)
-    print(json.dumps(line), flush=True)
+    # free this workload's device memory before the next one
+    del dev_batches, items, host, flush
+    scene.close()
+    bvh.close()
+    ctx.set_launch_params(**saved_params)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return line
 
 
-def run_batch_bench(args, rank: int, world: int, local_rank: int):
+SUB_KEYS = ("value", "unit", "ms_per_step", "steps", "warmup", "config", "setup", "roofline", "batches",
+            "e2e", "clocks", "gpu_launches")
+
+
+def run_engine(args, rank: int, world: int, local_rank: int):
+    import torch
+
+    import igx_raytracing_gb300 as igx
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = igx.Context(local_rank)
+    if args.layout is not None:
+        ctx.set_launch_params(layout=args.layout)
+    line = measure_plain(args, ctx, dev, args.workload, world)
+    # the benchmark spec's other targets under the same run: the 1M- and
+    # 2M-triangle incoherent workloads (the roofline target is on the 1M
+    # variant), the 64-scene batch against 64 plain launches, and a serving run
+    if args.workload == "sphere" and world == 1 and not args.no_extras:
+        for sub in ("incoherent1m", "incoherent"):
+            log(f"bench: {sub}")
+            s = measure_plain(args, ctx, dev, sub, world, lite=True)
+            line[sub] = {k: s[k] for k in SUB_KEYS if k in s}
+        line["incoherent1m"]["target"] = {
+            "what": "roofline.frac >= 0.5 on 1M random triangles with 4M incoherent rays",
+            "met": bool(line["incoherent1m"]["roofline"]["frac"] >= 0.5)}
+        log("bench: batch")
+        line["batch"] = measure_batch(args, ctx, dev, world)
+        log("bench: serve")
+        line["serve"] = measure_serve(args, ctx, local_rank, world, args.serve_seconds)
+        line["gpu_launches"] += (line["incoherent1m"]["gpu_launches"] + line["incoherent"]["gpu_launches"]
+                                 + line["batch"]["gpu_launches"] + line["serve"]["gpu_launches"])
+        line["sub_objects"] = ("incoherent1m, incoherent, batch and serve: each measured in this run with "
+                               "its own clock record; gpu_launches counts every timed launch of all of them")
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_batch(args, ctx, dev, world: int) -> dict:
     """64 scenes (triangles log-uniform in [1K, 512K]) with ray batches
     log-uniform in [4K, 2M] (half pinhole primaries, half incoherent): one
     autotuned, graph-captured persistent launch against 64 sequential plain
     launches of the same items on one stream."""
     import torch
 
-    import igx_raytracing_gb300 as igx
     from igx_raytracing_gb300 import BVH, scenes
+    from igx_raytracing_gb300.dist import max_over_ranks
 
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    ctx = igx.Context(local_rank)
     ntris, nrays = scenes.workload_batch_plan(64)
     t0 = time.perf_counter()
-    items, host_rays, bvhs = [], [], []
+    items, host_rays, owned = [], [], []
     for i, (nt, nr) in enumerate(zip(ntris, nrays)):
         tris = scenes.random_triangles(int(nt), scenes.seed_for(4, i))
         bvh = BVH.build(tris)
         scene = ctx.create_scene(bvh=bvh)
+        bvh.close()
         rays = scenes.batch_rays(i, int(nr))
         d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
         out = torch.empty((len(rays), 4), dtype=torch.float32, device=dev)
         items.append((scene, d_rays, None, out, 0))
         host_rays.append(rays)
-        bvhs.append(bvh)
+        owned.append(scene)
     setup_s = time.perf_counter() - t0
     total_rays = int(sum(len(r) for r in host_rays))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    plain_params = ctx.launch_params
 
     t0 = time.perf_counter()
     tuned, tuned_ms = ctx.autotune(items, reps=2, force=True)
     tune_s = time.perf_counter() - t0
-    plain_params = ctx.launch_params
 
     def timed(fn, steps):
         ts = []
@@ -658,16 +744,16 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
     ctx.set_launch_params(**tuned)
     seq_tuned_ms = statistics.mean(timed(sequential, args.steps))
     ctx.set_launch_params(**plain_params)
-    clocks = ClockSampler(local_rank)
+    clocks = ClockSampler(dev.index or 0, tag="_batch")
     clocks.start()
     region = timed_region_start()
     bat = timed(batch.launch, args.steps)
     timed_region_end(region)
     clk = clocks.stop()
-    bat_ms = statistics.mean(bat)
+    bat_ms = max_over_ranks(statistics.mean(bat), dev)
     ctx.sync()
     # the batch's results equal the plain launches' (checked bit for bit here
-    # on a few items; the test suite checks every item)
+    # on a few items; the test suite checks items against the oracle)
     # (compared as integers: a miss stores prim 0xFFFFFFFF, a NaN bit pattern)
     ref = [items[i][3].clone() for i in range(0, 64, 16)]
     sequential()
@@ -692,9 +778,6 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
     batch_h = ctx.create_batch([(it[0], hr, None, hh, 0) for it, hr, hh in zip(items, pinned, hits_host)],
                                params=tuned)
 
-    def e2e():
-        batch_h.launch()
-
     def copied():
         for (scene, d_rays, _, out, _), hr in zip(items, pinned):
             d_rays.copy_(hr, non_blocking=True)
@@ -702,63 +785,108 @@ def run_batch_bench(args, rank: int, world: int, local_rank: int):
         for (scene, d_rays, _, out, _), hh in zip(items, hits_host):
             hh.copy_(out, non_blocking=True)
 
-    e2e_ms = statistics.mean(timed(e2e, args.steps))
+    e2e_ms = statistics.mean(timed(batch_h.launch, args.steps))
     same_h = all(torch.equal(hh.view(torch.int32), out.cpu().view(torch.int32))
                  for (_, _, _, out, _), hh in zip(items, hits_host))
     copied_ms = statistics.mean(timed(copied, args.steps))
     batch_h.close()
+    batch.close()
+    wl = "batch_64_scenes_1k_512k_tris_4k_2m_rays"
+    out = {"value": round(world * total_rays / (bat_ms / 1e3) / 1e6, 3), "unit": UNIT,
+           "ms_per_step": round(bat_ms, 4), "steps": args.steps, "warmup": args.warmup,
+           "config": {"workload": wl, "scenes": 64, "triangles": int(ntris.sum()),
+                      "rays_per_step": total_rays, "l2": L2_NOTE},
+           "setup": {"autotuned": tuned, "autotune_s": round(tune_s, 2), "setup_s": round(setup_s, 1)},
+           "plain_sequential": {"ms_per_step": round(seq_ms, 4),
+                                "mrays_s": round(total_rays / (seq_ms / 1e3) / 1e6, 3), "params": plain_params},
+           "plain_sequential_tuned": {"ms_per_step": round(seq_tuned_ms, 4),
+                                      "mrays_s": round(total_rays / (seq_tuned_ms / 1e3) / 1e6, 3)},
+           "batched_over_plain": round(seq_ms / bat_ms, 3),
+           "batched_over_plain_tuned": round(seq_tuned_ms / bat_ms, 3),
+           "target": {"what": "one batched launch faster than 64 sequential plain launches",
+                      "met": bool(seq_ms > bat_ms)},
+           "results_equal_plain": bool(same),
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                        "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                        "traffic": traffic_from_profiles(wl, "batch", layout),
+                        "kernel": f"batch_kernel<{LAYOUT_NAMES[layout]}>", "peak_source": peaks["source"],
+                        "bytes_per_launch": int(bytes_total)},
+           "e2e": {"value": round(world * total_rays / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
+                   "h2d_bytes_per_step": total_rays * RAY_BYTES,
+                   "d2h_bytes_per_step": total_rays * HIT_BYTES, "ms_per_step": round(e2e_ms, 3),
+                   "route": "batch items in pinned host memory, read and written in place by the kernel",
+                   "results_equal_device_batch": bool(same_h),
+                   "copied": {"value": round(world * total_rays / (copied_ms / 1e3) / 1e6, 3),
+                              "ms_per_step": round(copied_ms, 3),
+                              "route": "rays copied up, device batch, hits copied down"}},
+           "gpu_launches": args.steps,
+           "clocks": clk}
+    del items, pinned, hits_host, flush
+    for s in owned:
+        s.close()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_batch_bench(args, rank: int, world: int, local_rank: int):
+    import torch
+
+    import igx_raytracing_gb300 as igx
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = igx.Context(local_rank)
+    out = measure_batch(args, ctx, dev, world)
+    ctx.close()
     if rank != 0:
         return
-    value = world * total_rays / (bat_ms / 1e3) / 1e6
-    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(bat_ms, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": "batch_64_scenes_1k_512k_tris_4k_2m_rays", "scenes": 64,
-                       "triangles": int(ntris.sum()), "rays_per_step": total_rays,
-                       "autotuned": tuned, "autotune_s": round(tune_s, 2),
-                       "setup_s": round(setup_s, 1),
-                       "l2": "256 MiB buffer written between timed steps"},
-            "plain_sequential": {"ms_per_step": round(seq_ms, 4),
-                                 "mrays_s": round(total_rays / (seq_ms / 1e3) / 1e6, 3),
-                                 "params": plain_params},
-            "plain_sequential_tuned": {"ms_per_step": round(seq_tuned_ms, 4),
-                                       "mrays_s": round(total_rays / (seq_tuned_ms / 1e3) / 1e6, 3)},
-            "batched_over_plain": round(seq_ms / bat_ms, 3),
-            "batched_over_plain_tuned": round(seq_tuned_ms / bat_ms, 3),
-            "results_equal_plain": bool(same),
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
-                         "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
-                         "traffic": traffic_from_profiles("batch_64_scenes_1k_512k_tris_4k_2m_rays", "batch", layout),
-                         "kernel": f"batch_kernel<{LAYOUT_NAMES[layout]}>",
-                         "peak_source": peaks["source"]},
-            "e2e": {"value": round(world * total_rays / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
-                    "h2d_bytes_per_step": total_rays * RAY_BYTES,
-                    "d2h_bytes_per_step": total_rays * HIT_BYTES, "ms_per_step": round(e2e_ms, 3),
-                    "route": "batch items in pinned host memory, read and written in place by the kernel",
-                    "results_equal_device_batch": bool(same_h),
-                    "copied": {"value": round(world * total_rays / (copied_ms / 1e3) / 1e6, 3),
-                               "ms_per_step": round(copied_ms, 3),
-                               "route": "rays copied up, device batch, hits copied down"}},
-            "gpu_launches": args.steps,
-            "clocks": clk}
+    line = {"metric": METRIC, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic"}
+    line.update(out)
     print(json.dumps(line), flush=True)
 
 
-def run_serve_bench(args, rank: int, world: int, local_rank: int):
+def _device_overlap(times) -> dict:
+    """From the batch kernels' own %globaltimer intervals: pairs of batches on
+    different streams that ran at the same time, and the time during which
+    two or more batch kernels ran."""
+    iv = sorted((int(t["start_ns"]), int(t["end_ns"]), int(t["stream"])) for t in times)
+    pairs = 0
+    for i in range(len(iv)):
+        for j in range(i + 1, len(iv)):
+            if iv[j][0] >= iv[i][1]:
+                break
+            pairs += iv[j][2] != iv[i][2]
+    events = sorted([(s, 1) for s, _, _ in iv] + [(e, -1) for _, e, _ in iv])
+    depth, last, busy, multi = 0, 0, 0, 0
+    for t, d in events:
+        if depth >= 1:
+            busy += t - last
+        if depth >= 2:
+            multi += t - last
+        depth += d
+        last = t
+    return {"batches": len(iv), "overlapping_pairs": int(pairs), "busy_ms": round(busy / 1e6, 3),
+            "two_or_more_kernels_ms": round(multi / 1e6, 3),
+            "source": "each batch kernel's first CTA start and last warp exit (%globaltimer), "
+                      "igxrt_server_batch_times"}
+
+
+def measure_serve(args, ctx, device: int, world: int, duration: float) -> dict:
     """32 resident scenes (10K-2M triangles), Poisson arrivals at `--rate`
-    requests/s for `--duration` s; each request names a scene, 1K-1M rays
-    (log-uniform), closest or any hit.  The engine's server (admission under a
-    24 GiB cap, continuous batching over 3 streams) against a plain server
-    that traces each request with one plain kernel launch in arrival order,
-    both fed the same request stream."""
+    requests/s for `duration` s; each request names a scene, 1K-1M rays
+    (log-uniform), closest or any hit.  The requests are submitted by the
+    server's native pacer (igxrt_server_replay) at their scheduled arrival
+    times, and latency runs from that time to the results in host memory.
+    The engine's server (admission under a 24 GiB cap, continuous batching,
+    large requests sliced) against a plain server that traces each request
+    with one launch in arrival order, both fed the same request stream."""
     import torch
 
     import igx_raytracing_gb300 as igx
     from igx_raytracing_gb300 import BVH, scenes
 
-    torch.cuda.set_device(local_rank)
-    ctx = igx.Context(local_rank)
     rng = np.random.default_rng(scenes.seed_for(5))
     ntris = scenes.log_uniform_ints(rng, 10_000, 2_000_000, 32)
     t0 = time.perf_counter()
@@ -767,83 +895,61 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
     for i, nt in enumerate(ntris):
         bvh = BVH.build(scenes.random_triangles(int(nt), scenes.seed_for(5, i)))
         sc.append(ctx.create_scene(bvh=bvh))
+        bvh.close()
         r = scenes.batch_rays(1000 + i, pool_rays)
         pr = torch.empty(pool_rays * 8, dtype=torch.float32).pin_memory().numpy()
         pr[:] = r.view(np.float32).reshape(-1)
         pools.append(pr.view(igx.RAY_DTYPE))
     setup_s = time.perf_counter() - t0
     # the request stream
-    n_req = int(args.rate * args.duration)
+    n_req = int(args.rate * duration)
     gaps = rng.exponential(1.0 / args.rate, n_req)
     arrivals = np.cumsum(gaps)
     scene_of = rng.integers(0, 32, n_req)
     counts = scenes.log_uniform_ints(rng, 1000, 1_000_000, n_req)
     modes = rng.integers(0, 2, n_req)
     offsets = rng.integers(0, pool_rays - counts + 1)
-    out_ring = torch.empty(64 << 20, dtype=torch.float32).pin_memory().numpy()  # 256 MiB
+    # results land in a pinned ring of 1 GiB (several hundred ms of results
+    # at the offered rate; nothing here reads them back)
+    out_ring = torch.empty(256 << 20, dtype=torch.float32).pin_memory().numpy()
     ring_words = len(out_ring)
 
-    def out_for(k, pos):
-        words = int(counts[k]) * (4 if modes[k] == 0 else 1)
-        pos = (pos + 3) & ~3  # hit records need 16-byte alignment
-        if pos + words > ring_words:
-            pos = 0
-        view = out_ring[pos:pos + words]
-        return (view.view(igx.HIT_DTYPE) if modes[k] == 0 else view.view(np.uint32)), pos + words
-
-    def client(submit):
-        pos = 0
-        start = time.perf_counter()
+    def requests(ids):
+        reqs, pos = [], 0
         for k in range(n_req):
-            due = start + arrivals[k]
-            while True:
-                d = due - time.perf_counter()
-                if d <= 0:
-                    break
-                if d > 0.0005:
-                    time.sleep(d - 0.0004)
-            out, pos = out_for(k, pos)
+            words = int(counts[k]) * (4 if modes[k] == 0 else 1)
+            pos = (pos + 3) & ~3  # hit records need 16-byte alignment
+            if pos + words > ring_words:
+                pos = 0
+            view = out_ring[pos:pos + words]
+            pos += words
+            out = view.view(igx.HIT_DTYPE) if modes[k] == 0 else view.view(np.uint32)
             rays = pools[scene_of[k]][offsets[k]:offsets[k] + counts[k]]
-            submit(k, rays, out)
+            reqs.append((ids[scene_of[k]], rays, None, int(modes[k]), out))
+        return reqs
 
-    def serve_pass(streams: int, max_batch_requests: int, with_clocks: bool):
-        srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=streams,
-                         max_batch_requests=max_batch_requests)
+    def serve_pass(opts: dict, with_clocks: bool):
+        srv = igx.Server(ctx, memory_cap_bytes=24 << 30, **opts)
         ids = [srv.add_scene(s) for s in sc]
-        for k in range(8):  # warm-up requests
+        for k in range(8):  # warm-up requests on a server of their own
             srv.wait(srv.submit(ids[k], pools[k][:50000], None, k % 2))
         srv.close()
-        srv = igx.Server(ctx, memory_cap_bytes=24 << 30, streams=streams,
-                         max_batch_requests=max_batch_requests)
+        srv = igx.Server(ctx, memory_cap_bytes=24 << 30, **opts)
         ids = [srv.add_scene(s) for s in sc]
-        tickets = [0] * n_req
-        clocks = ClockSampler(local_rank, interval_ms=250)
+        reqs = requests(ids)
+        clocks = ClockSampler(device, interval_ms=250, tag="_serve")
         if with_clocks:
             clocks.start()
-
-        def submit_srv(k, rays, out):
-            tickets[k] = srv.submit(ids[scene_of[k]], rays, None, int(modes[k]), out=out)
-
-        client(submit_srv)
+        tickets = srv.replay(reqs, arrivals)
         lat = np.zeros(n_req)
         for k, t in enumerate(tickets):
             w = srv.wait(t)
-            lat[k] = 1e3 * (w["completed"] - w["submitted"])
+            lat[k] = 1e3 * (w["completed"] - w["arrival"])
         clk = clocks.stop() if with_clocks else None
         st = srv.stats()
+        times = srv.batch_times()
         srv.close()
-        return st, lat, clk
-
-    # the client thread spins between arrivals: keep its GIL slices short
-    sys.setswitchinterval(1e-4)
-    # engine: continuous batching, `streams` batches in flight
-    st, srv_lat, clk = serve_pass(args.streams, 0, True)
-    span = st["last_complete"] - st["first_submit"]
-    served = st["rays_completed"] / span / 1e6
-    # plain: the same native server launching one request at a time, in
-    # arrival order, one launch in flight (no coalescing, no overlap)
-    pst, plain_lat, _ = serve_pass(1, 1, False)
-    plain_span = pst["last_complete"] - pst["first_submit"]
+        return st, lat, clk, times
 
     def classes(lat):
         out = {}
@@ -854,37 +960,65 @@ def run_serve_bench(args, rank: int, world: int, local_rank: int):
                              "p99_ms": round(float(np.percentile(lat[m], 99)), 3)}
         return out
 
-    plain = {"p50_ms": round(pst["p50_ms"], 3), "p99_ms": round(pst["p99_ms"], 3),
-             "mrays_s": round(pst["rays_completed"] / plain_span / 1e6, 3),
-             "batches": pst["batches"], "by_size": classes(plain_lat),
-             "mode": "same server, one request per launch, one launch in flight"}
-    if rank != 0:
-        return
+    engine_opts = {"streams": args.streams}
+    st, srv_lat, clk, times = serve_pass(engine_opts, True)
+    span = st["last_complete"] - st["first_submit"]
+    served = st["rays_completed"] / span / 1e6
+    # plain: the same native server launching one whole request at a time, in
+    # arrival order, one launch in flight (no coalescing, slicing or overlap)
+    plain_opts = {"streams": 1, "max_batch_requests": 1, "slice_rays": 0xFFFFFFFF}
+    pst, plain_lat, _, _ = serve_pass(plain_opts, False)
+    plain_span = pst["last_complete"] - pst["first_submit"]
     offered = float(counts.sum()) / float(arrivals[-1]) / 1e6
-    line = {"metric": METRIC, "value": round(served, 3), "unit": UNIT, "n_gpus": world,
-            "steps": n_req, "warmup": 8, "ms_per_step": round(1e3 * span / n_req, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {"workload": "serve_32_scenes_poisson", "scenes": 32,
-                       "triangles": int(ntris.sum()), "rate_req_s": args.rate,
-                       "duration_s": args.duration, "requests": n_req,
+    for s in sc:
+        s.close()
+    return {"value": round(world * served, 3), "unit": UNIT,
+            "config": {"workload": "serve_32_scenes_poisson", "scenes": 32, "triangles": int(ntris.sum()),
+                       "rate_req_s": args.rate, "duration_s": duration, "requests": n_req,
                        "rays_offered": int(counts.sum()), "offered_mrays_s": round(offered, 3),
-                       "memory_cap_gib": 24, "streams": args.streams, "setup_s": round(setup_s, 1),
-                       "launch": ctx.launch_params},
+                       "memory_cap_gib": 24},
+            "setup": {"setup_s": round(setup_s, 1), "launch": ctx.launch_params,
+                      "server": dict(engine_opts, slice_rays="default (256K)", max_batch_rays="default (1M)")},
+            "latency_from": "each request's scheduled arrival time (submitted by the server's native "
+                            "pacer, igxrt_server_replay) to its results in host memory",
             "serving": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
                         "mean_ms": round(st["mean_ms"], 3), "max_ms": round(st["max_ms"], 3),
-                        "batches": st["batches"], "requests_per_batch": round(n_req / max(1, st["batches"]), 2),
-                        "peak_memory_gib": round(st["peak_memory_bytes"] / 2**30, 3),
-                        "peak_pending": st["peak_pending"],
-                        "peak_in_flight_batches": st["peak_in_flight_batches"],
-                        "rejected": st["rejected"], "by_size": classes(srv_lat)},
-            "plain_server": plain,
-            "e2e": {"value": round(served, 3), "unit": UNIT,
+                        "batches": st["batches"], "peak_memory_gib": round(st["peak_memory_bytes"] / 2**30, 3),
+                        "peak_pending": st["peak_pending"], "rejected": st["rejected"],
+                        "by_size": classes(srv_lat)},
+            "device_overlap": _device_overlap(times),
+            "plain_server": {"p50_ms": round(pst["p50_ms"], 3), "p99_ms": round(pst["p99_ms"], 3),
+                             "mrays_s": round(pst["rays_completed"] / plain_span / 1e6, 3),
+                             "batches": pst["batches"], "by_size": classes(plain_lat),
+                             "mode": "same server, one whole request per launch, one launch in flight"},
+            "e2e": {"value": round(world * served, 3), "unit": UNIT,
                     "h2d_bytes_per_step": int(counts.sum() * RAY_BYTES // n_req),
                     "d2h_bytes_per_step": int(sum(int(c) * (HIT_BYTES if m == 0 else OCC_BYTES)
-                                                  for c, m in zip(counts, modes)) // n_req)},
-            "gpu_launches": st["batches"],
+                                                  for c, m in zip(counts, modes)) // n_req),
+                    "route": "requests from pinned host memory through the server (copies, batched "
+                             "launch, copies back), per request"},
+            "gpu_launches": int(st["batches"]),
             "clocks": clk}
+
+
+def run_serve_bench(args, rank: int, world: int, local_rank: int):
+    import torch
+
+    import igx_raytracing_gb300 as igx
+
+    torch.cuda.set_device(local_rank)
+    ctx = igx.Context(local_rank)
+    # the client thread's GIL slices stay short while the native pacer runs
+    sys.setswitchinterval(1e-4)
+    out = measure_serve(args, ctx, local_rank, world, args.duration)
+    ctx.close()
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "n_gpus": world, "steps": out["config"]["requests"], "warmup": 8,
+            "ms_per_step": round(1e3 * args.duration / max(1, out["config"]["requests"]), 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic"}
+    line.update(out)
     print(json.dumps(line), flush=True)
 
 
@@ -1253,6 +1387,14 @@ def run_dynamic_bench(args, rank: int, world: int, local_rank: int):
         print(json.dumps(line), flush=True)
 
 
+def _free_port() -> int:
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1265,15 +1407,27 @@ def main():
     ap.add_argument("--layout", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="sphere: leave out the incoherent, batch and serve sub-objects")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="sphere: seconds of arrivals in the serve sub-object")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--streams", type=int, default=2, help="serve: batches in flight")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        # start one rank per GPU (the launch the driver uses for N > 1)
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
+               os.path.abspath(__file__)] + sys.argv[1:]
+        raise SystemExit(subprocess.call(cmd))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus:
+        raise SystemExit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}: launch one rank per GPU")
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

@@ -182,7 +182,7 @@ def check(status: int, ctx=None, what: str = "") -> None:
 class ServerOptions(C.Structure):
     _fields_ = [("memory_cap_bytes", C.c_uint64), ("max_batch_rays", C.c_uint32),
                 ("max_batch_requests", C.c_uint32), ("streams", C.c_uint32),
-                ("reserved", C.c_uint32 * 3)]
+                ("slice_rays", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class Request(C.Structure):
@@ -193,7 +193,13 @@ class Request(C.Structure):
 
 class RequestStats(C.Structure):
     _fields_ = [("submitted", C.c_double), ("admitted", C.c_double), ("launched", C.c_double),
-                ("completed", C.c_double), ("batch", C.c_uint32), ("status", C.c_uint32)]
+                ("completed", C.c_double), ("batch", C.c_uint32), ("status", C.c_uint32),
+                ("arrival", C.c_double)]
+
+
+class BatchTime(C.Structure):
+    _fields_ = [("start_ns", C.c_uint64), ("end_ns", C.c_uint64), ("batch", C.c_uint32),
+                ("stream", C.c_uint32), ("rays", C.c_uint64)]
 
 
 class ServerStats(C.Structure):
@@ -209,7 +215,10 @@ PROTOTYPES += [
     ("igxrt_server_create", _st, [_vp, C.POINTER(ServerOptions), C.POINTER(_vp)]),
     ("igxrt_server_add_scene", _st, [_vp, _vp, C.POINTER(_u32)]),
     ("igxrt_server_submit", _st, [_vp, C.POINTER(Request), C.POINTER(_u64)]),
+    ("igxrt_server_replay", _st, [_vp, C.POINTER(Request), C.POINTER(C.c_double), _u32,
+                                  C.POINTER(_u64)]),
     ("igxrt_server_wait", _st, [_vp, _u64, C.c_double, C.POINTER(RequestStats)]),
+    ("igxrt_server_batch_times", _st, [_vp, C.POINTER(BatchTime), _u32, C.POINTER(_u32)]),
     ("igxrt_server_get_stats", _st, [_vp, C.POINTER(ServerStats)]),
     ("igxrt_server_destroy", _st, [_vp]),
 ]

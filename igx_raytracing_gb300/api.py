@@ -599,10 +599,10 @@ class Server:
     request has been waited for."""
 
     def __init__(self, ctx: Context, memory_cap_bytes: int = 0, max_batch_rays: int = 0,
-                 max_batch_requests: int = 0, streams: int = 0):
+                 max_batch_requests: int = 0, streams: int = 0, slice_rays: int = 0):
         o = _capi.ServerOptions()
         o.memory_cap_bytes, o.max_batch_rays = memory_cap_bytes, max_batch_rays
-        o.max_batch_requests, o.streams = max_batch_requests, streams
+        o.max_batch_requests, o.streams, o.slice_rays = max_batch_requests, streams, slice_rays
         h = C.c_void_p()
         check(lib().igxrt_server_create(ctx.handle, C.byref(o), C.byref(h)), ctx.handle,
               "server_create")
@@ -615,20 +615,54 @@ class Server:
         check(lib().igxrt_server_add_scene(self._h, scene.handle, C.byref(sid)), what="add_scene")
         return sid.value
 
-    def submit(self, scene_id: int, rays, prev_hit=None, mode: int = 0, out=None) -> int:
+    @staticmethod
+    def _request(q, scene_id: int, rays, prev_hit, mode: int, out):
         r = as_rays(rays)
         prev = None if prev_hit is None else np.ascontiguousarray(prev_hit, dtype=np.uint32)
         if out is None:
             out = np.empty(len(r), dtype=HIT_DTYPE) if mode == 0 else np.empty(len(r), dtype=np.uint32)
-        q = _capi.Request()
         q.scene_id, q.mode, q.count = scene_id, mode, len(r)
         q.rays = r.ctypes.data if len(r) else None
         q.prev_hit = prev.ctypes.data if prev is not None else None
         q.out = out.ctypes.data if len(r) else None
+        return (r, prev, out)
+
+    def submit(self, scene_id: int, rays, prev_hit=None, mode: int = 0, out=None) -> int:
+        q = _capi.Request()
+        keep = Server._request(q, scene_id, rays, prev_hit, mode, out)
         t = C.c_uint64()
         check(lib().igxrt_server_submit(self._h, C.byref(q), C.byref(t)), what="server_submit")
-        self._keep[t.value] = (r, prev, out)
+        self._keep[t.value] = keep
         return t.value
+
+    def replay(self, requests, arrivals) -> list:
+        """igxrt_server_replay: requests = [(scene_id, rays, prev_hit, mode,
+        out)], submitted natively at arrivals[i] seconds after the call starts;
+        each request's latency counts from that scheduled time.  Returns the
+        tickets (0 for a request refused at admission)."""
+        n = len(requests)
+        arr = (_capi.Request * max(n, 1))()
+        keep = [Server._request(arr[i], *req) for i, req in enumerate(requests)]
+        times = np.ascontiguousarray(arrivals, dtype=np.float64)
+        assert len(times) == n
+        tickets = (C.c_uint64 * max(n, 1))()
+        check(lib().igxrt_server_replay(self._h, arr, times.ctypes.data_as(C.POINTER(C.c_double)), n,
+                                        tickets), what="server_replay")
+        out = [int(tickets[i]) for i in range(n)]
+        for t, k in zip(out, keep):
+            if t:
+                self._keep[t] = k
+        return out
+
+    def batch_times(self, max_batches: int = 1 << 20) -> np.ndarray:
+        """igxrt_server_batch_times: (start_ns, end_ns, batch, stream, rays) of
+        every completed batch kernel, from %globaltimer on the device."""
+        buf = (_capi.BatchTime * max_batches)()
+        n = C.c_uint32()
+        check(lib().igxrt_server_batch_times(self._h, buf, max_batches, C.byref(n)), what="batch_times")
+        dt = np.dtype([("start_ns", "<u8"), ("end_ns", "<u8"), ("batch", "<u4"), ("stream", "<u4"),
+                       ("rays", "<u8")])
+        return np.frombuffer(bytes(buf)[: n.value * C.sizeof(_capi.BatchTime)], dtype=dt).copy()
 
     def wait(self, ticket: int, timeout: float = -1.0) -> dict:
         s = _capi.RequestStats()
@@ -637,7 +671,7 @@ class Server:
             raise IgxrtError(st, f"request {ticket}")
         kept = self._keep.pop(ticket, None)
         return {"submitted": s.submitted, "admitted": s.admitted, "launched": s.launched,
-                "completed": s.completed, "batch": s.batch,
+                "completed": s.completed, "arrival": s.arrival, "batch": s.batch,
                 "out": kept[2] if kept is not None else None}
 
     def stats(self) -> dict:

@@ -125,7 +125,8 @@ struct Timer {
         std::vector<BatchItemDev> table;
         uint32_t packets = 0;
         uint64_t rays = 0;
-        if (build_batch_table(ctx, items, count, p, table, packets, rays) != IGXRT_OK)
+        bool mixed = false;
+        if (build_batch_table(ctx, items, count, p, table, packets, rays, mixed) != IGXRT_OK)
             return -1.f;
         if (!table.empty() &&
             cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(BatchItemDev),
@@ -134,7 +135,7 @@ struct Timer {
         std::vector<float> ts;
         for (uint32_t r = 0; r < reps + 1; ++r) {
             cudaEventRecord(e0, stream);
-            if (launch_batch(ctx, d_table, count, packets, rays, p, queue, stream) != IGXRT_OK)
+            if (launch_batch(ctx, d_table, count, packets, rays, p, queue, stream, mixed) != IGXRT_OK)
                 return -1.f;
             cudaEventRecord(e1, stream);
             if (cudaEventSynchronize(e1) != cudaSuccess)

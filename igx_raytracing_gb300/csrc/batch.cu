@@ -22,7 +22,7 @@
 
 namespace igxrt {
 
-static_assert(sizeof(BatchItemDev) == 56, "batch item layout");
+static_assert(sizeof(BatchItemDev) == 72, "batch item layout");
 
 struct BatchArgs {
     const BatchItemDev* items;
@@ -33,16 +33,26 @@ struct BatchArgs {
     uint32_t packet;
     uint32_t sh_depth;
     uint32_t refill_lanes;
+    unsigned long long* times;  // optional: {earliest CTA start, latest warp exit}
 };
 
-// A finished ray's record: occluded word (any hit) or hit (closest).
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// A finished ray's record: occluded word (any hit) or hit (closest).  Mixed
+// scenes keep a priority code in best.prim (traverse.cuh), decoded here.
+template <bool MIXED>
 __device__ __forceinline__ void write_result(void* out, uint32_t mode, uint32_t ray, const RayState& r,
                                              const BestHit& best, bool occluded) {
     if (mode) {
         __stcs(static_cast<uint32_t*>(out) + ray, occluded ? 1u : 0u);
     } else {
-        const bool hit = best.t < r.tmax_eff;
-        const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(best.prim))
+        const bool hit = MIXED ? (best.t < r.tmax_eff || best.prim < kPrioNone) : best.t < r.tmax_eff;
+        const uint32_t prim = MIXED ? id_of_prio(best.prim) : best.prim;
+        const float4 h = hit ? make_float4(best.t, best.u, best.v, __uint_as_float(prim))
                              : make_float4(IGXRT_NO_HIT, 0.f, 0.f, __uint_as_float(IGXRT_NO_RAY_HIT));
         __stcs(static_cast<float4*>(out) + ray, h);
     }
@@ -63,8 +73,13 @@ struct BatchLane {
     }
 };
 
-template <int LAYOUT>
+// MIXED: items may hold spheres, cubes and planes (typed leaves, planes tested
+// when a ray starts, priority-coded best hit); triangle-only items trace the
+// same in it.
+template <int LAYOUT, bool MIXED>
 __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
+    if (a.times && threadIdx.x == 0)
+        atomicMin(a.times, global_ns());
     extern __shared__ uint32_t smem[];
     TraversalStack st;
     st.sh = reinterpret_cast<uint2*>(smem) + threadIdx.x;
@@ -77,7 +92,7 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
     uint32_t w_item = 0, w_base = 0, w_end = 0;
     bool queue_done = false;
     // lane state
-    bool alive = false;
+    bool alive = false, occluded_at_start = false;
     uint32_t ray = 0, mode = 0;
     const float4* nodes = nullptr;
     const float4* prims = nullptr;
@@ -92,7 +107,8 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         if (queue_done && __ballot_sync(0xffffffffu, !alive || (link & (kLinkWait | kLinkMerge))) != 0) {
             BatchLane lane_item{nodes, prims, out, mode};
             share_tail<kSharePerLane>(lane, lower, link, alive, ray, r, best, st, next, lane_item,
-                                      [&](bool occ) { write_result(out, mode, ray, r, best, occ); });
+                                      [&](bool occ) { write_result<MIXED>(out, mode, ray, r, best, occ); },
+                                      MIXED ? kPrioNone : 0u);
         }
         const uint32_t idle = __ballot_sync(0xffffffffu, !alive);
         const uint32_t nidle = __popc(idle);
@@ -139,9 +155,19 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
                     best.t = r.tmax_eff;
                     best.u = 0.f;
                     best.v = 0.f;
-                    best.prim = 0;
+                    best.prim = MIXED ? kPrioNone : 0u;
                     best.tcull = cull_limit(best.t);
                     next = it->node_count ? 0 : kRefDone;
+                    occluded_at_start = false;
+                    if (MIXED) {
+                        const uint32_t np = it->plane_count;
+                        if (np) {
+                            occluded_at_start = mode ? test_planes<true>(it->planes, np, it->plane_base, r, best)
+                                                     : test_planes<false>(it->planes, np, it->plane_base, r, best);
+                            if (occluded_at_start)
+                                next = kRefDone;
+                        }
+                    }
                     st.sp = 0;
                     alive = true;
                 }
@@ -154,11 +180,18 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         if (alive && !(link & (kLinkWait | kLinkMerge))) {
             bool overflow = false;
             while (next >= 0 && next != kRefDone)
-                next = visit_node<LAYOUT, false>(nodes, next, r, best, st, overflow, unused);
-            bool occluded = false;
+                next = visit_node<LAYOUT, false, MIXED>(nodes, next, r, best, st, overflow, unused);
+            // a plane occluding the ray at its start decides it in this first
+            // round only (the lane may next help another ray in the tail)
+            bool occluded = occluded_at_start;
+            occluded_at_start = false;
             if (next < 0) {
-                occluded = mode ? process_leaf<true, false>(prims, next, r, best, unused)
-                                : process_leaf<false, false>(prims, next, r, best, unused);
+                if (MIXED)
+                    occluded = mode ? process_leaf_mixed<true>(prims, next, r, best)
+                                    : process_leaf_mixed<false>(prims, next, r, best);
+                else
+                    occluded = mode ? process_leaf<true, false>(prims, next, r, best, unused)
+                                    : process_leaf<false, false>(prims, next, r, best, unused);
                 if (!occluded)
                     next = st.pop_live(best.tcull);
             }
@@ -169,20 +202,23 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
                     // share_tail writes the ray once no helper of it remains
                     link |= ((link & 31u) == lane ? kLinkWait : kLinkMerge) | (occluded ? kLinkOcc : 0u);
                 } else {
-                    write_result(out, mode, ray, r, best, occluded);
+                    write_result<MIXED>(out, mode, ray, r, best, occluded);
                     alive = false;
                 }
             }
         }
     }
+    if (a.times && lane == 0)
+        atomicMax(a.times + 1, global_ns());
 }
 
 using BatchFn = void (*)(BatchArgs);
 
-static BatchFn select_batch_kernel(uint32_t layout) {
-    if (layout == IGXRT_LAYOUT_BVH8)
-        return batch_kernel<IGXRT_LAYOUT_BVH8>;
-    return layout == IGXRT_LAYOUT_BVH4 ? batch_kernel<IGXRT_LAYOUT_BVH4> : batch_kernel<IGXRT_LAYOUT_BVH2>;
+static BatchFn select_batch_kernel(uint32_t layout, bool mixed) {
+    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
+    if (mixed)
+        return layout == B8 ? batch_kernel<B8, true> : layout == B4 ? batch_kernel<B4, true> : batch_kernel<B2, true>;
+    return layout == B8 ? batch_kernel<B8, false> : layout == B4 ? batch_kernel<B4, false> : batch_kernel<B2, false>;
 }
 
 namespace {
@@ -191,23 +227,37 @@ bool aligned(const void* p, size_t a) { return ((uintptr_t)p % a) == 0; }
 
 }  // namespace
 
+void batch_item_for(const igxrt_scene* scene, const igxrt_launch_params& p, const igxrt_ray* rays,
+                    const uint32_t* prev, void* out, uint32_t count, uint32_t mode, BatchItemDev& d) {
+    d.nodes = reinterpret_cast<const float4*>(scene->nodes[p.layout]);
+    d.prims = reinterpret_cast<const float4*>(scene->prims);
+    d.rays = rays;
+    d.prev = prev;
+    d.out = out;
+    d.planes = reinterpret_cast<const float4*>(scene->planes);
+    d.count = count;
+    d.mode = mode;
+    d.node_count = scene->node_count[p.layout];
+    d.packet_begin = 0;
+    d.plane_count = scene->plane_count;
+    d.plane_base = scene->plane_base;
+}
+
 igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,
                                const igxrt_launch_params& p, std::vector<BatchItemDev>& table,
-                               uint32_t& total_packets, uint64_t& total_rays) {
+                               uint32_t& total_packets, uint64_t& total_rays, bool& mixed) {
     if (count && !items)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "items is NULL");
     table.resize(count);
     uint64_t packets = 0;
     total_rays = 0;
+    mixed = false;
     for (uint32_t i = 0; i < count; ++i) {
         const igxrt_batch_item& it = items[i];
         if (!it.scene)
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: scene is NULL", i));
         if (it.scene->device != ctx->device)
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, format("item %u: scene on another device", i));
-        if (it.scene->mixed)
-            return fail(ctx, IGXRT_ERROR_UNSUPPORTED,
-                        format("item %u: batches take triangle-only scenes", i));
         if (!it.scene->has_layout(p.layout))
             return fail(ctx, IGXRT_ERROR_UNSUPPORTED, format("item %u: the scene has no layout %u", i, p.layout));
         if (it.mode > 1)
@@ -223,15 +273,9 @@ igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items
             return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                         format("item %u: batch arrays must be device memory", i));
         BatchItemDev& d = table[i];
-        d.nodes = reinterpret_cast<const float4*>(it.scene->nodes[p.layout]);
-        d.prims = reinterpret_cast<const float4*>(it.scene->prims);
-        d.rays = it.rays;
-        d.prev = it.prev_hit;
-        d.out = it.out;
-        d.count = it.count;
-        d.mode = it.mode;
-        d.node_count = it.scene->node_count[p.layout];
+        batch_item_for(it.scene, p, it.rays, it.prev_hit, it.out, it.count, it.mode, d);
         d.packet_begin = (uint32_t)packets;
+        mixed |= it.scene->mixed;
         packets += (it.count + p.packet_size - 1) / p.packet_size;
         total_rays += it.count;
         if (packets >= 0x7fffffffu)
@@ -243,10 +287,10 @@ igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items
 
 igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint32_t count,
                           uint32_t total_packets, uint64_t total_rays, const igxrt_launch_params& p,
-                          uint32_t* queue, cudaStream_t stream) {
+                          uint32_t* queue, cudaStream_t stream, bool mixed, unsigned long long* times) {
     if (total_packets == 0)
         return IGXRT_OK;
-    BatchFn fn = select_batch_kernel(p.layout);
+    BatchFn fn = select_batch_kernel(p.layout, mixed);
     const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
     cudaError_t e = allow_smem((const void*)fn, smem);
@@ -271,6 +315,7 @@ igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint3
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;
+    a.times = times;
     e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "batch queue reset");
@@ -334,7 +379,8 @@ igxrt_status igxrt_trace_batch(igxrt_context* ctx, const igxrt_batch_item* items
     std::vector<BatchItemDev> table;
     uint32_t packets = 0;
     uint64_t rays = 0;
-    st = build_batch_table(ctx, items, count, p, table, packets, rays);
+    bool mixed = false;
+    st = build_batch_table(ctx, items, count, p, table, packets, rays, mixed);
     if (st != IGXRT_OK || packets == 0)
         return st;
     DeviceGuard guard(ctx->device);
@@ -351,7 +397,7 @@ igxrt_status igxrt_trace_batch(igxrt_context* ctx, const igxrt_batch_item* items
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "batch table upload");
     uint32_t* queue = take_queue_slot(ctx);
-    st = launch_batch(ctx, d_table, count, packets, rays, p, queue, stream);
+    st = launch_batch(ctx, d_table, count, packets, rays, p, queue, stream, mixed);
     if (st != IGXRT_OK)
         return st;
     // the ring's slots are zero between launches (trace launches skip the
@@ -376,7 +422,8 @@ igxrt_status igxrt_batch_create(igxrt_context* ctx, const igxrt_batch_item* item
     std::vector<BatchItemDev> table;
     uint32_t packets = 0;
     uint64_t rays = 0;
-    st = build_batch_table(ctx, items, count, p, table, packets, rays);
+    bool mixed = false;
+    st = build_batch_table(ctx, items, count, p, table, packets, rays, mixed);
     if (st != IGXRT_OK)
         return st;
     DeviceGuard guard(ctx->device);
@@ -404,7 +451,7 @@ igxrt_status igxrt_batch_create(igxrt_context* ctx, const igxrt_batch_item* item
         e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         st = launch_batch(ctx, static_cast<const BatchItemDev*>(b->d_mem), count, packets, rays, p,
-                          queue, cap);
+                          queue, cap, mixed);
         cudaGraph_t g = nullptr;
         const cudaError_t e2 = cudaStreamEndCapture(cap, &g);
         b->graph = g;

@@ -133,18 +133,33 @@ struct BatchItemDev {
     const igxrt_ray* rays;
     const uint32_t* prev;
     void* out;
+    const float4* planes;   // mixed scenes: the planes outside the tree (else NULL)
     uint32_t count;
     uint32_t mode;
     uint32_t node_count;
     uint32_t packet_begin;  // first packet of this item in the batch's packet space
+    uint32_t plane_count;
+    uint32_t plane_base;    // object id of the scene's first plane
 };
 
+// Fills the device table of `count` items; `mixed` is set when an item's
+// scene holds spheres, cubes or planes (the batch then runs the mixed kernel,
+// which traces triangle-only items as well).
 igxrt_status build_batch_table(igxrt_context* ctx, const igxrt_batch_item* items, uint32_t count,
                                const igxrt_launch_params& p, std::vector<BatchItemDev>& table,
-                               uint32_t& total_packets, uint64_t& total_rays);
+                               uint32_t& total_packets, uint64_t& total_rays, bool& mixed);
+// One item table entry for rays [first, first + count) of a scene (the
+// server's request slices); `rays`, `prev` and `out` already point at the
+// slice's first element.
+void batch_item_for(const igxrt_scene* scene, const igxrt_launch_params& p, const igxrt_ray* rays,
+                    const uint32_t* prev, void* out, uint32_t count, uint32_t mode, BatchItemDev& d);
+// `times` (optional, device memory): the earliest CTA start and the latest
+// warp exit of the launch, %globaltimer nanoseconds, folded in by atomicMin /
+// atomicMax (the caller sets them to ~0 and 0 first).
 igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint32_t count,
                           uint32_t total_packets, uint64_t total_rays, const igxrt_launch_params& p,
-                          uint32_t* queue, cudaStream_t stream);
+                          uint32_t* queue, cudaStream_t stream, bool mixed,
+                          unsigned long long* times = nullptr);
 
 // Next work-queue counter of the context (a ring of kQueueSlots words); the
 // slot's exit counter is exit_word(slot).

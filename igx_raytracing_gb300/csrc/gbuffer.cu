@@ -6,8 +6,9 @@
 // (res/shaders/camera.glsl:72-87, 113-116), the hit encoding of
 // raygen.comp:39-51, decodeSpheremap / interpolate / encodeNormal
 // (res/shaders/primitive.glsl:85-104, 146-151) for the vertex normal of
-// trace.glsl:48-57.  A warp covers an 8x4 pixel tile so neighbouring
-// primary rays traverse together.
+// trace.glsl:48-57 (for a sphere, cube or plane of a mixed scene, its
+// geometry normal, trace.glsl:59-63).  A warp covers an 8x4 pixel tile so
+// neighbouring primary rays traverse together.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -22,6 +23,10 @@ struct GbufferArgs {
     const float4* prims;
     uint32_t node_count;
     const igxrt_triangle* tris;
+    uint32_t tri_count;       // mixed scenes: objects below this id are triangles
+    const float4* planes;     // mixed scenes: planes outside the tree
+    uint32_t plane_count;
+    uint32_t plane_base;
     igxrt_camera cam;
     float inv_w, inv_h;
     uint32_t tiles_x, tiles;
@@ -85,7 +90,48 @@ __global__ void camera_rays_kernel(igxrt_camera c, float inv_w, float inv_h, flo
     rays[2 * i + 1] = make_float4(d.x, d.y, d.z, IGXRT_NO_HIT);
 }
 
-template <int LAYOUT>
+// geometryNormal of a non-triangle hit (primitive.glsl:190-192, 223, 311-327),
+// recomputed from the hit's record (or plane) with the shader's operations:
+// a sphere's normalize(centre - o) at o = hitT * dir + pos; a cube's axis
+// normal, +1 when the entry plane is the start plane; a plane's
+// normalize(n), negated when the ray runs along it (dif > 0).
+__device__ __forceinline__ float3 mixed_geometry_normal(const RayState& r, const float4* __restrict__ prims,
+                                                        const float4* __restrict__ planes, uint32_t rec,
+                                                        float t) {
+    if (rec & kRecPlane) {
+        const float4 pl = __ldg(planes + (rec & ~kRecPlane));
+        const float len = __fsqrt_rn(dot3(pl.x, pl.y, pl.z, pl.x, pl.y, pl.z));
+        const float nx = __fdiv_rn(pl.x, len), ny = __fdiv_rn(pl.y, len), nz = __fdiv_rn(pl.z, len);
+        const float dif = dot3(r.dx, r.dy, r.dz, -nx, -ny, -nz);
+        return dif > 0.f ? make_float3(-nx, -ny, -nz) : make_float3(nx, ny, nz);
+    }
+    const float4* p = prims + 3 * (size_t)rec;
+    const float4 v0 = __ldg(p), v1 = __ldg(p + 1), v2 = __ldg(p + 2);
+    if (__float_as_uint(v2.w) == kPrimSphere) {
+        const float ox = __fadd_rn(__fmul_rn(t, r.dx), r.ox), oy = __fadd_rn(__fmul_rn(t, r.dy), r.oy),
+                    oz = __fadd_rn(__fmul_rn(t, r.dz), r.oz);
+        const float nx = __fsub_rn(v0.x, ox), ny = __fsub_rn(v0.y, oy), nz = __fsub_rn(v0.z, oz);
+        const float len = __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz));
+        return make_float3(__fdiv_rn(nx, len), __fdiv_rn(ny, len), __fdiv_rn(nz, len));
+    }
+    // cube {start, id}{end, leaf_end}: the entry distances of cube_hit
+    const float rx = __frcp_rn(r.dx), ry = __frcp_rn(r.dy), rz = __frcp_rn(r.dz);
+    const float sx = __fmul_rn(__fsub_rn(v0.x, r.ox), rx), sy = __fmul_rn(__fsub_rn(v0.y, r.oy), ry),
+                sz = __fmul_rn(__fsub_rn(v0.z, r.oz), rz);
+    const float ex = __fmul_rn(__fsub_rn(v1.x, r.ox), rx), ey = __fmul_rn(__fsub_rn(v1.y, r.oy), ry),
+                ez = __fmul_rn(__fsub_rn(v1.z, r.oz), rz);
+    const float mix = gmin(sx, ex), miy = gmin(sy, ey), miz = gmin(sz, ez);
+    const float tmin = gmax(gmax(mix, miy), miz);
+    if (tmin == mix)
+        return make_float3(mix == sx ? 1.f : -1.f, 0.f, 0.f);
+    if (tmin == miy)
+        return make_float3(0.f, miy == sy ? 1.f : -1.f, 0.f);
+    return make_float3(0.f, 0.f, miz == sz ? 1.f : -1.f);
+}
+
+// MIXED: scenes with spheres, cubes and planes; the object normal of a
+// non-triangle hit is its geometry normal (trace.glsl:59-63).
+template <int LAYOUT, bool MIXED>
 __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
     extern __shared__ uint32_t smem[];
     TraversalStack st;
@@ -122,14 +168,26 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
         r.prev = IGXRT_NO_RAY_HIT;
         BestHit best;
         bool overflow = false;
-        trace_single<LAYOUT, false>(a.nodes, a.prims, a.node_count, r, best, st, overflow);
+        uint32_t rec = 0;
+        if (MIXED)
+            trace_single_mixed<LAYOUT>(a.nodes, a.prims, a.node_count, a.planes, a.plane_count, a.plane_base, r,
+                                       best, st, overflow, rec);
+        else
+            trace_single<LAYOUT, false>(a.nodes, a.prims, a.node_count, r, best, st, overflow);
         if (overflow)
             atomicOr(a.status, kStatusStackOverflow);
         const size_t px = (size_t)y * c.width + x;
+        // raygen.comp:39-44: a miss is hitT == noHit
         if (best.t < IGXRT_NO_HIT) {
+            const uint32_t object = MIXED ? id_of_prio(best.prim) : best.prim;
             a.dir_object[px] = make_float4(__fmul_rn(dx, best.t), __fmul_rn(dy, best.t),
-                                           __fmul_rn(dz, best.t), __uint_as_float(best.prim));
-            const igxrt_triangle& t = a.tris[best.prim];
+                                           __fmul_rn(dz, best.t), __uint_as_float(object));
+            if (MIXED && object >= a.tri_count) {
+                const uint2 e = encode_normal(mixed_geometry_normal(r, a.prims, a.planes, rec, best.t));
+                a.uv_normal[px] = make_float4(best.u, best.v, __uint_as_float(e.x), __uint_as_float(e.y));
+                continue;
+            }
+            const igxrt_triangle& t = a.tris[object];
             const float3 n0 = decode_spheremap(t.n0), n1 = decode_spheremap(t.n1),
                          n2 = decode_spheremap(t.n2);
             // interpolate(n0, n1, n2, uv): (u*n1 + v*n2) + (1 - u - v)*n0
@@ -158,8 +216,6 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     igxrt_status st = check_scene(ctx, scene);
     if (st != IGXRT_OK)
         return st;
-    if (scene->mixed)
-        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "the G-buffer pass takes triangle-only scenes");
     if (!cam || !dir_object || !uv_normal)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "camera and both images must be non-NULL");
     if (!cam->width || !cam->height)
@@ -208,6 +264,10 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     a.prims = reinterpret_cast<const float4*>(scene->prims);
     a.node_count = scene->node_count[p.layout];
     a.tris = scene->tris;
+    a.tri_count = scene->info.triangle_count;
+    a.planes = reinterpret_cast<const float4*>(scene->planes);
+    a.plane_count = scene->plane_count;
+    a.plane_base = scene->plane_base;
     a.cam = *cam;
     a.inv_w = 1.0f / (float)cam->width;
     a.inv_h = 1.0f / (float)cam->height;
@@ -217,9 +277,11 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     a.uv_normal = d_uv;
     a.status = status_word(ctx);
     a.sh_depth = p.stack_depth;
-    auto fn = p.layout == IGXRT_LAYOUT_BVH8   ? gbuffer_kernel<IGXRT_LAYOUT_BVH8>
-              : p.layout == IGXRT_LAYOUT_BVH4 ? gbuffer_kernel<IGXRT_LAYOUT_BVH4>
-                                              : gbuffer_kernel<IGXRT_LAYOUT_BVH2>;
+    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
+    auto fn = scene->mixed ? (p.layout == B8 ? gbuffer_kernel<B8, true>
+                              : p.layout == B4 ? gbuffer_kernel<B4, true> : gbuffer_kernel<B2, true>)
+                           : (p.layout == B8 ? gbuffer_kernel<B8, false>
+                              : p.layout == B4 ? gbuffer_kernel<B4, false> : gbuffer_kernel<B2, false>);
     const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
     cudaError_t e = allow_smem((const void*)fn, smem);

@@ -9,15 +9,22 @@
 //      result buffers fit into a device arena of `memory_cap_bytes` (one
 //      cudaMalloc at start; sub-allocated first-fit, 256-byte aligned);
 //   2. continuous batching: whenever one of `streams` stream slots is free,
-//      every admitted request not yet launched (up to max_batch_rays /
-//      max_batch_requests) is coalesced into one batched persistent launch
-//      on that stream: uploads, the kernel, downloads, an event;
-//   3. completion: finished events release the requests' arena blocks (so
-//      waiting requests can be admitted) and wake their waiters.
+//      the admitted requests with rays not yet launched are coalesced into
+//      one batched persistent launch on that stream (uploads, the kernel,
+//      downloads, an event), each request with its next slice of at most
+//      `slice_rays` rays, up to max_batch_rays per launch.  A large request
+//      therefore spreads over several launches, each shared with the requests
+//      queued behind it, instead of making them wait for all of its rays;
+//   3. completion: finished events account each slice; a request whose
+//      slices are all done releases its arena block (so waiting requests can
+//      be admitted) and wakes its waiters.
 // Requests that arrive while batches run are admitted and launched on the
-// next free slot, so their work overlaps the running batches on the device.
-// Every ray's result depends only on its own scene and ray, so a request's
-// results are the same alone or in any mix.
+// next free slot, so their work overlaps the running batches on the device;
+// each batch kernel stamps its first start and last exit with %globaltimer,
+// which igxrt_server_batch_times reports.  Latency runs from a request's
+// arrival: its scheduled time when igxrt_server_replay paces it, else its
+// submission.  Every ray's result depends only on its own scene and ray, so
+// a request's results are the same alone, sliced, or in any mix.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -89,7 +96,15 @@ struct Request {
     uint64_t ticket = 0;
     size_t bytes = 0, offset = 0;
     igxrt_request_stats st{};
+    uint32_t launched_rays = 0;  // rays handed to batches (scheduler thread)
+    uint32_t done_rays = 0;      // rays whose batch has completed
     bool done = false;
+};
+
+// Rays [first, first + count) of a request, carried by one batch.
+struct Slice {
+    Request* q;
+    uint32_t first, count;
 };
 
 struct Slot {
@@ -98,7 +113,11 @@ struct Slot {
     BatchItemDev* d_table = nullptr;
     BatchItemDev* h_table = nullptr;  // pinned
     uint32_t* queue = nullptr;
-    std::vector<Request*> reqs;
+    unsigned long long* d_times = nullptr;  // {first CTA start, last warp exit}
+    unsigned long long* h_times = nullptr;  // pinned copy, read at completion
+    std::vector<Slice> slices;
+    uint32_t seq = 0;
+    uint64_t rays = 0;
     bool busy = false;
 };
 
@@ -123,8 +142,9 @@ struct igxrt_server {
     std::vector<double> latencies_ms;
     igxrt_server_stats stats{};
 
-    std::deque<Request*> ready;  // admitted, not launched (scheduler thread only)
+    std::deque<Request*> ready;  // admitted, rays left to launch (scheduler thread only)
     uint32_t batch_seq = 0;
+    std::vector<igxrt_batch_time> batch_times;  // completed batches (under mu)
     std::thread worker;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -132,6 +152,7 @@ struct igxrt_server {
     void admit();
     bool launch_one();
     bool complete();
+    igxrt_status submit(const igxrt_request* req, double arrival, uint64_t* ticket);
 };
 
 void igxrt_server::admit() {
@@ -160,52 +181,67 @@ bool igxrt_server::launch_one() {
         }
     if (!s)
         return false;
-    s->reqs.clear();
+    s->slices.clear();
     uint64_t rays = 0;
     uint32_t packets = 0;
-    while (!ready.empty() && s->reqs.size() < opt.max_batch_requests) {
-        Request* q = ready.front();
-        if (!s->reqs.empty() && rays + q->r.count > opt.max_batch_rays)
+    bool mixed = false;
+    // every request in the ready queue, in order, adds its next slice
+    for (auto it = ready.begin(); it != ready.end() && s->slices.size() < opt.max_batch_requests;) {
+        Request* q = *it;
+        const uint32_t n = std::min(q->r.count - q->launched_rays, opt.slice_rays);
+        if (!s->slices.empty() && rays + n > opt.max_batch_rays)
             break;
-        ready.pop_front();
+        const uint32_t first = q->launched_rays;
         const igxrt_scene* sc = scenes[q->r.scene_id];
         char* base = d_arena + q->offset;
         const size_t rb = round256((size_t)q->r.count * sizeof(igxrt_ray));
         const size_t pb = q->r.prev_hit ? round256((size_t)q->r.count * 4) : 0;
-        BatchItemDev& d = s->h_table[s->reqs.size()];
-        d.nodes = reinterpret_cast<const float4*>(sc->nodes[params.layout]);
-        d.prims = reinterpret_cast<const float4*>(sc->prims);
-        d.rays = reinterpret_cast<const igxrt_ray*>(base);
-        d.prev = q->r.prev_hit ? reinterpret_cast<const uint32_t*>(base + rb) : nullptr;
-        d.out = base + rb + pb;
-        d.count = q->r.count;
-        d.mode = q->r.mode;
-        d.node_count = sc->node_count[params.layout];
+        const size_t elem = q->r.mode ? sizeof(uint32_t) : sizeof(igxrt_hit);
+        igxrt_ray* d_rays = reinterpret_cast<igxrt_ray*>(base) + first;
+        uint32_t* d_prev = q->r.prev_hit ? reinterpret_cast<uint32_t*>(base + rb) + first : nullptr;
+        BatchItemDev& d = s->h_table[s->slices.size()];
+        batch_item_for(sc, params, d_rays, d_prev, base + rb + pb + (size_t)first * elem, n, q->r.mode, d);
         d.packet_begin = packets;
-        packets += (q->r.count + params.packet_size - 1) / params.packet_size;
-        rays += q->r.count;
-        cudaMemcpyAsync(base, q->r.rays, (size_t)q->r.count * sizeof(igxrt_ray),
-                        cudaMemcpyHostToDevice, s->stream);
+        packets += (n + params.packet_size - 1) / params.packet_size;
+        rays += n;
+        mixed |= sc->mixed;
+        cudaMemcpyAsync(d_rays, q->r.rays + first, (size_t)n * sizeof(igxrt_ray), cudaMemcpyHostToDevice,
+                        s->stream);
         if (q->r.prev_hit)
-            cudaMemcpyAsync(base + rb, q->r.prev_hit, (size_t)q->r.count * 4, cudaMemcpyHostToDevice,
-                            s->stream);
-        s->reqs.push_back(q);
+            cudaMemcpyAsync(d_prev, q->r.prev_hit + first, (size_t)n * 4, cudaMemcpyHostToDevice, s->stream);
+        s->slices.push_back({q, first, n});
+        q->launched_rays += n;
+        if (q->launched_rays == q->r.count)
+            it = ready.erase(it);
+        else
+            ++it;
     }
-    const uint32_t n = (uint32_t)s->reqs.size();
+    const uint32_t n = (uint32_t)s->slices.size();
     const uint32_t seq = ++batch_seq;
     cudaMemcpyAsync(s->d_table, s->h_table, n * sizeof(BatchItemDev), cudaMemcpyHostToDevice, s->stream);
-    igxrt_status st = launch_batch(ctx, s->d_table, n, packets, rays, params, s->queue, s->stream);
+    cudaMemsetAsync(s->d_times, 0xff, sizeof(unsigned long long), s->stream);
+    cudaMemsetAsync(s->d_times + 1, 0, sizeof(unsigned long long), s->stream);
+    igxrt_status st = launch_batch(ctx, s->d_table, n, packets, rays, params, s->queue, s->stream, mixed,
+                                   s->d_times);
     const double t = now();
-    for (Request* q : s->reqs) {
+    for (const Slice& sl : s->slices) {
+        Request* q = sl.q;
         const size_t rb = round256((size_t)q->r.count * sizeof(igxrt_ray));
         const size_t pb = q->r.prev_hit ? round256((size_t)q->r.count * 4) : 0;
-        const size_t ob = (size_t)q->r.count * (q->r.mode ? sizeof(uint32_t) : sizeof(igxrt_hit));
-        cudaMemcpyAsync(q->r.out, d_arena + q->offset + rb + pb, ob, cudaMemcpyDeviceToHost, s->stream);
-        q->st.launched = t;
+        const size_t elem = q->r.mode ? sizeof(uint32_t) : sizeof(igxrt_hit);
+        cudaMemcpyAsync(static_cast<char*>(q->r.out) + (size_t)sl.first * elem,
+                        d_arena + q->offset + rb + pb + (size_t)sl.first * elem, (size_t)sl.count * elem,
+                        cudaMemcpyDeviceToHost, s->stream);
+        if (sl.first == 0)
+            q->st.launched = t;
         q->st.batch = seq;
-        q->st.status = st;
+        if (st != IGXRT_OK)
+            q->st.status = st;
     }
+    cudaMemcpyAsync(s->h_times, s->d_times, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->stream);
     cudaEventRecord(s->event, s->stream);
+    s->seq = seq;
+    s->rays = rays;
     s->busy = true;
     {
         std::lock_guard<std::mutex> lock(mu);
@@ -220,7 +256,8 @@ bool igxrt_server::launch_one() {
 
 bool igxrt_server::complete() {
     bool any = false;
-    for (auto& s : slots) {
+    for (size_t k = 0; k < slots.size(); ++k) {
+        Slot& s = slots[k];
         if (!s.busy)
             continue;
         const cudaError_t e = cudaEventQuery(s.event);
@@ -228,18 +265,29 @@ bool igxrt_server::complete() {
             continue;
         const double t = now();
         std::lock_guard<std::mutex> lock(mu);
-        for (Request* q : s.reqs) {
-            arena->release(q->offset, q->bytes);
-            q->st.completed = t;
+        igxrt_batch_time bt{};
+        bt.start_ns = s.h_times[0];
+        bt.end_ns = s.h_times[1];
+        bt.batch = s.seq;
+        bt.stream = (uint32_t)k;
+        bt.rays = s.rays;
+        batch_times.push_back(bt);
+        for (const Slice& sl : s.slices) {
+            Request* q = sl.q;
             if (e != cudaSuccess)
                 q->st.status = IGXRT_ERROR_CUDA;
+            q->done_rays += sl.count;
+            if (q->done_rays < q->r.count)
+                continue;
+            arena->release(q->offset, q->bytes);
+            q->st.completed = t;
             q->done = true;
             stats.completed++;
             stats.rays_completed += q->r.count;
             stats.last_complete = t;
-            latencies_ms.push_back(1e3 * (t - q->st.submitted));
+            latencies_ms.push_back(1e3 * (t - q->st.arrival));
         }
-        s.reqs.clear();
+        s.slices.clear();
         s.busy = false;
         any = true;
     }
@@ -274,6 +322,47 @@ void igxrt_server::run() {
     }
 }
 
+igxrt_status igxrt_server::submit(const igxrt_request* req, double arrival, uint64_t* ticket) {
+    std::unique_ptr<Request> q(new (std::nothrow) Request());
+    if (!q)
+        return IGXRT_ERROR_OUT_OF_MEMORY;
+    q->r = *req;
+    const double t = now();
+    q->st.submitted = t;
+    q->st.arrival = arrival < 0 ? t : arrival;
+    std::lock_guard<std::mutex> lock(mu);
+    if (req->scene_id >= scenes.size() || req->mode > 1 || (req->count && (!req->rays || !req->out)))
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    if (((uintptr_t)req->rays % 16) || ((uintptr_t)req->prev_hit % 4) || ((uintptr_t)req->out % 4))
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    q->bytes = round256((size_t)req->count * sizeof(igxrt_ray)) +
+               (req->prev_hit ? round256((size_t)req->count * 4) : 0) +
+               round256((size_t)req->count * (req->mode ? sizeof(uint32_t) : sizeof(igxrt_hit)));
+    stats.submitted++;
+    if (stats.first_submit < 0)
+        stats.first_submit = t;
+    if (q->bytes > opt.memory_cap_bytes) {
+        stats.rejected++;
+        return IGXRT_ERROR_ADMISSION;
+    }
+    q->ticket = next_ticket++;
+    *ticket = q->ticket;
+    Request* raw = q.get();
+    reqs.emplace(q->ticket, std::move(q));
+    if (raw->r.count == 0) {
+        raw->st.admitted = raw->st.launched = raw->st.completed = t;
+        raw->done = true;
+        stats.completed++;
+        latencies_ms.push_back(1e3 * (t - raw->st.arrival));
+        cv_done.notify_all();
+        return IGXRT_OK;
+    }
+    pending.push_back(raw);
+    stats.peak_pending = std::max<uint32_t>(stats.peak_pending, (uint32_t)pending.size());
+    cv_work.notify_one();
+    return IGXRT_OK;
+}
+
 extern "C" {
 
 igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options* opts, igxrt_server** out) {
@@ -289,7 +378,9 @@ igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options*
     if (!s->opt.memory_cap_bytes)
         s->opt.memory_cap_bytes = 24ull << 30;
     if (!s->opt.max_batch_rays)
-        s->opt.max_batch_rays = 4u << 20;
+        s->opt.max_batch_rays = 1u << 20;
+    if (!s->opt.slice_rays)
+        s->opt.slice_rays = 256u << 10;
     if (!s->opt.max_batch_requests)
         s->opt.max_batch_requests = 1024;
     if (!s->opt.streams)
@@ -309,19 +400,22 @@ igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options*
     s->arena.reset(new Arena(s->opt.memory_cap_bytes));
     s->slots.resize(s->opt.streams);
     for (auto& sl : s->slots) {
+        // item table, then the queue word, then the two timestamps, 256 bytes apart
         const size_t tb = round256(s->opt.max_batch_requests * sizeof(BatchItemDev));
         e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess)
             e = cudaEventCreateWithFlags(&sl.event, cudaEventDisableTiming);
         if (e == cudaSuccess)
-            e = cudaMalloc(&sl.d_table, tb + 256);
+            e = cudaMalloc(&sl.d_table, tb + 512);
         if (e == cudaSuccess)
-            e = cudaMallocHost(&sl.h_table, tb);
+            e = cudaMallocHost(&sl.h_table, tb + 256);
         if (e != cudaSuccess) {
             igxrt_server_destroy(s.release());
             return cuda_fail(ctx, e, "server stream slots");
         }
         sl.queue = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(sl.d_table) + tb);
+        sl.d_times = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(sl.d_table) + tb + 256);
+        sl.h_times = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(sl.h_table) + tb);
     }
     s->t0 = Clock::now();
     s->stats.first_submit = -1;
@@ -336,9 +430,9 @@ igxrt_status igxrt_server_add_scene(igxrt_server* s, const igxrt_scene* scene, u
         return IGXRT_ERROR_INVALID_ARGUMENT;
     if (scene->device != s->ctx->device)
         return IGXRT_ERROR_INVALID_ARGUMENT;
-    // the batched kernel the server launches traces triangle-only trees in
-    // the server's layout
-    if (scene->mixed || !scene->has_layout(s->params.layout))
+    // the batched kernel traces the tree in the server's layout (mixed
+    // scenes run its mixed variant)
+    if (!scene->has_layout(s->params.layout))
         return IGXRT_ERROR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(s->mu);
     *scene_id = (uint32_t)s->scenes.size();
@@ -349,42 +443,28 @@ igxrt_status igxrt_server_add_scene(igxrt_server* s, const igxrt_scene* scene, u
 igxrt_status igxrt_server_submit(igxrt_server* s, const igxrt_request* req, uint64_t* ticket) {
     if (!s || !req || !ticket)
         return IGXRT_ERROR_INVALID_ARGUMENT;
-    std::unique_ptr<Request> q(new (std::nothrow) Request());
-    if (!q)
-        return IGXRT_ERROR_OUT_OF_MEMORY;
-    q->r = *req;
-    const double t = s->now();
-    q->st.submitted = t;
-    std::lock_guard<std::mutex> lock(s->mu);
-    if (req->scene_id >= s->scenes.size() || req->mode > 1 || (req->count && (!req->rays || !req->out)))
+    return s->submit(req, -1.0, ticket);
+}
+
+igxrt_status igxrt_server_replay(igxrt_server* s, const igxrt_request* reqs, const double* arrival_s,
+                                 uint32_t count, uint64_t* tickets) {
+    if (!s || (count && (!reqs || !arrival_s || !tickets)))
         return IGXRT_ERROR_INVALID_ARGUMENT;
-    if (((uintptr_t)req->rays % 16) || ((uintptr_t)req->prev_hit % 4) || ((uintptr_t)req->out % 4))
-        return IGXRT_ERROR_INVALID_ARGUMENT;
-    q->bytes = round256((size_t)req->count * sizeof(igxrt_ray)) +
-               (req->prev_hit ? round256((size_t)req->count * 4) : 0) +
-               round256((size_t)req->count * (req->mode ? sizeof(uint32_t) : sizeof(igxrt_hit)));
-    s->stats.submitted++;
-    if (s->stats.first_submit < 0)
-        s->stats.first_submit = t;
-    if (q->bytes > s->opt.memory_cap_bytes) {
-        s->stats.rejected++;
-        return IGXRT_ERROR_ADMISSION;
+    const double start = s->now();
+    for (uint32_t i = 0; i < count; ++i) {
+        const double due = start + arrival_s[i];
+        for (;;) {
+            const double d = due - s->now();
+            if (d <= 0)
+                break;
+            if (d > 300e-6)
+                std::this_thread::sleep_for(std::chrono::duration<double>(d - 200e-6));
+        }
+        tickets[i] = 0;
+        const igxrt_status st = s->submit(&reqs[i], due, &tickets[i]);
+        if (st != IGXRT_OK && st != IGXRT_ERROR_ADMISSION)
+            return st;
     }
-    q->ticket = s->next_ticket++;
-    *ticket = q->ticket;
-    Request* raw = q.get();
-    s->reqs.emplace(q->ticket, std::move(q));
-    if (raw->r.count == 0) {
-        raw->st.admitted = raw->st.launched = raw->st.completed = t;
-        raw->done = true;
-        s->stats.completed++;
-        s->latencies_ms.push_back(0.0);
-        s->cv_done.notify_all();
-        return IGXRT_OK;
-    }
-    s->pending.push_back(raw);
-    s->stats.peak_pending = std::max<uint32_t>(s->stats.peak_pending, (uint32_t)s->pending.size());
-    s->cv_work.notify_one();
     return IGXRT_OK;
 }
 
@@ -427,6 +507,17 @@ igxrt_status igxrt_server_get_stats(igxrt_server* s, igxrt_server_stats* out) {
             sum += x;
         out->mean_ms = sum / l.size();
     }
+    return IGXRT_OK;
+}
+
+igxrt_status igxrt_server_batch_times(igxrt_server* s, igxrt_batch_time* out, uint32_t max_batches,
+                                      uint32_t* count) {
+    if (!s || !count || (max_batches && !out))
+        return IGXRT_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(s->mu);
+    const uint32_t n = (uint32_t)std::min<size_t>(max_batches, s->batch_times.size());
+    std::copy(s->batch_times.begin(), s->batch_times.begin() + n, out);
+    *count = n;
     return IGXRT_OK;
 }
 

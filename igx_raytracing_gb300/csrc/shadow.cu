@@ -94,8 +94,6 @@ extern "C" igxrt_status igxrt_trace_shadow_mask(igxrt_context* ctx, const igxrt_
     igxrt_status st = check_scene(ctx, scene);
     if (st != IGXRT_OK)
         return st;
-    if (scene->mixed)
-        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "the shadow pass takes triangle-only scenes");
     if (!width || !height || !samples)
         return IGXRT_OK;
     const uint64_t pixels = (uint64_t)width * height, nrays = pixels * samples;

@@ -88,6 +88,11 @@ extern "C" igxrt_status igxrt_trace_closest_static(igxrt_context* ctx, const igx
     igxrt_status st = resolve_params(ctx, ctx->params, p);
     if (st != IGXRT_OK)
         return st;
+    // a tree without the context's layout (a GPU-built scene has no BVH8)
+    // would trace every ray as a miss: refuse it as igxrt_trace_closest does
+    if (!scene->has_layout(p.layout))
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED,
+                    format("the scene has no layout %u (GPU-built trees have BVH2 and BVH4)", p.layout));
     DeviceGuard guard(ctx->device);
     if (!guard.ok())
         return fail(ctx, IGXRT_ERROR_CUDA, "cannot select the context's device");

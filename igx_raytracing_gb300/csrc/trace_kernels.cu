@@ -179,7 +179,11 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
             // node phase
             while (next >= 0 && next != kRefDone)
                 next = visit_node<LAYOUT, COUNT, MIXED>(a.nodes, next, r, best, st, overflow, nf);
+            // a plane occluding the ray when it started decides it in this
+            // first round; the flag must not outlive the ray (the lane may
+            // next help another ray's traversal in the tail)
             bool occluded = occluded_at_start;
+            occluded_at_start = false;
             // leaf phase
             if (next < 0) {
                 occluded = MIXED ? process_leaf_mixed<ANY, COUNT>(a.prims, next, r, best, &pf)
@@ -246,18 +250,28 @@ static KernelFn select_kernel(uint32_t layout, bool any, bool count, bool mixed)
     return any ? trace_kernel<B2, true, false, false> : trace_kernel<B2, false, false, false>;
 }
 
-igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
-                          const igxrt_launch_params& p, cudaStream_t stream) {
-    if (req.count == 0)
-        return IGXRT_OK;
+namespace {
+
+// The launch shape and arguments every traversal launch shares: the kernel
+// for the scene and query, its shared stack, a persistent grid of at most the
+// resident CTAs (fewer when the rays need fewer warps), and the scene, ray
+// and output pointers.  The caller adds the work-queue, error and exit words.
+struct TraceLaunch {
+    KernelFn fn = nullptr;
+    size_t smem = 0;
+    uint32_t grid = 0;
+    KernelArgs a{};
+};
+
+igxrt_status prepare_trace(igxrt_context* ctx, const TraceRequest& req, const igxrt_launch_params& p,
+                           TraceLaunch& l) {
     const igxrt_scene* s = req.scene;
-    const bool count = req.node_fetches != nullptr;
-    KernelFn fn = select_kernel(p.layout, req.mode == 1, count, s->mixed);
-    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
+    l.fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr, s->mixed);
+    l.smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
-    cudaError_t e = allow_smem((const void*)fn, smem);
+    cudaError_t e = allow_smem((const void*)l.fn, l.smem);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, l.fn, (int)p.block_size, l.smem);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "occupancy query");
     if (per_sm < 1)
@@ -266,10 +280,9 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
         per_sm = std::min(per_sm, (int)p.ctas_per_sm);
     const uint64_t warps_needed = ((uint64_t)req.count + p.packet_size - 1) / p.packet_size;
     const uint64_t ctas_needed = (warps_needed + p.block_size / 32 - 1) / (p.block_size / 32);
-    const uint32_t grid = (uint32_t)std::max<uint64_t>(
-        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, ctas_needed));
+    l.grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, ctas_needed));
 
-    KernelArgs a;
+    KernelArgs& a = l.a;
     a.nodes = reinterpret_cast<const float4*>(s->nodes[p.layout]);
     a.prims = reinterpret_cast<const float4*>(s->prims);
     a.node_count = s->node_count[p.layout];
@@ -281,30 +294,47 @@ igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
     a.occluded = req.occluded;
     a.node_fetches = req.node_fetches;
     a.prim_fetches = req.prim_fetches;
-    a.queue = take_queue_slot(ctx);
-    a.status = status_word(ctx);
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;
     a.planes = reinterpret_cast<const float4*>(s->planes);
     a.plane_count = s->plane_count;
     a.plane_base = s->plane_base;
+    a.queue = nullptr;
+    a.status = nullptr;
+    a.exit_count = nullptr;
+    a.independent = 0u;
+    return IGXRT_OK;
+}
+
+}  // namespace
+
+igxrt_status launch_trace(igxrt_context* ctx, const TraceRequest& req,
+                          const igxrt_launch_params& p, cudaStream_t stream) {
+    if (req.count == 0)
+        return IGXRT_OK;
+    TraceLaunch l;
+    igxrt_status st = prepare_trace(ctx, req, p, l);
+    if (st != IGXRT_OK)
+        return st;
+    l.a.queue = take_queue_slot(ctx);
+    l.a.status = status_word(ctx);
     // the slot's words are zero (zeroed at context creation, and by the last
     // warp of the slot's previous launch), so no reset sits between this
     // launch and the kernel before it
-    a.exit_count = exit_word(a.queue);
-    a.independent = req.independent ? 1u : 0u;
+    l.a.exit_count = exit_word(l.a.queue);
+    l.a.independent = req.independent ? 1u : 0u;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
+    cfg.gridDim = dim3(l.grid);
     cfg.blockDim = dim3(p.block_size);
-    cfg.dynamicSmemBytes = smem;
+    cfg.dynamicSmemBytes = l.smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, fn, a);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, l.fn, l.a);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "trace kernel launch");
     return IGXRT_OK;
@@ -315,47 +345,14 @@ igxrt_status launch_trace_words(igxrt_context* ctx, const TraceRequest& req,
                                 uint32_t* queue, uint32_t* status) {
     if (req.count == 0)
         return IGXRT_OK;
-    const igxrt_scene* s = req.scene;
-    KernelFn fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr, s->mixed);
-    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
-    int per_sm = 0;
-    cudaError_t e = allow_smem((const void*)fn, smem);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
-    if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "occupancy query");
-    if (per_sm < 1)
-        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "launch parameters leave no resident CTA");
-    if (p.ctas_per_sm)
-        per_sm = std::min(per_sm, (int)p.ctas_per_sm);
-    const uint64_t warps_needed = ((uint64_t)req.count + p.packet_size - 1) / p.packet_size;
-    const uint64_t ctas_needed = (warps_needed + p.block_size / 32 - 1) / (p.block_size / 32);
-    const uint32_t grid = (uint32_t)std::max<uint64_t>(
-        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, ctas_needed));
-    KernelArgs a;
-    a.nodes = reinterpret_cast<const float4*>(s->nodes[p.layout]);
-    a.prims = reinterpret_cast<const float4*>(s->prims);
-    a.node_count = s->node_count[p.layout];
-    a.rays = req.rays;
-    a.prev = req.prev;
-    a.count = req.count;
-    a.count_dev = req.count_dev;
-    a.hits = req.hits;
-    a.occluded = req.occluded;
-    a.node_fetches = req.node_fetches;
-    a.prim_fetches = req.prim_fetches;
-    a.queue = queue;
-    a.status = status;
-    a.exit_count = nullptr;  // the caller resets its words
-    a.independent = 0u;
-    a.packet = p.packet_size;
-    a.sh_depth = p.stack_depth;
-    a.refill_lanes = p.refill_lanes;
-    a.planes = reinterpret_cast<const float4*>(s->planes);
-    a.plane_count = s->plane_count;
-    a.plane_base = s->plane_base;
-    fn<<<grid, p.block_size, smem, stream>>>(a);
-    e = cudaGetLastError();
+    TraceLaunch l;
+    igxrt_status st = prepare_trace(ctx, req, p, l);
+    if (st != IGXRT_OK)
+        return st;
+    l.a.queue = queue;
+    l.a.status = status;  // the caller resets both words; no exit counter
+    l.fn<<<l.grid, p.block_size, l.smem, stream>>>(l.a);
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "trace kernel launch");
     return IGXRT_OK;

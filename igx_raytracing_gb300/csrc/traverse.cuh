@@ -514,7 +514,13 @@ __device__ __forceinline__ bool sphere_hit(const RayState& r, float cx, float cy
     return !(Q2 > R2);
 }
 
-// The sphere's uv (primitive.glsl:189-204); asin/atan are CUDA's.
+// The sphere's uv (primitive.glsl:189-204).  asin and atan give the
+// correctly rounded binary32 value: evaluated in binary64 (CUDA's asin /
+// atan, a few binary64 ulp) and rounded once, which lands on the correctly
+// rounded float unless the binary64 value falls within its error of a
+// binary32 rounding midpoint.  The oracle evaluates them the same way, so u
+// and v, which cancel towards 0 near the poles and the seam (lat * 1/pi +
+// 0.5), come out bit for bit instead of many float ulp apart.
 __device__ __forceinline__ void sphere_uv(const RayState& r, float cx, float cy, float cz, float hitT,
                                           float& u, float& v) {
     const float ox = __fadd_rn(__fmul_rn(hitT, r.dx), r.ox), oy = __fadd_rn(__fmul_rn(hitT, r.dy), r.oy),
@@ -522,8 +528,8 @@ __device__ __forceinline__ void sphere_uv(const RayState& r, float cx, float cy,
     const float nx = __fsub_rn(cx, ox), ny = __fsub_rn(cy, oy), nz = __fsub_rn(cz, oz);
     const float len = __fsqrt_rn(dot3f(nx, ny, nz, nx, ny, nz));
     const float ux = __fdiv_rn(nx, len), uy = __fdiv_rn(ny, len), uz = __fdiv_rn(nz, len);
-    const float lat = asinf(uz);
-    float lon = atanf(__fdiv_rn(uy, ux));
+    const float lat = __double2float_rn(asin((double)uz));
+    float lon = __double2float_rn(atan((double)__fdiv_rn(uy, ux)));
     if (lon != lon)
         lon = 0.f;
     const float k = (float)(0.636619746685 * 0.5);
@@ -587,9 +593,12 @@ __device__ __forceinline__ void plane_uv(const RayState& r, const float4& pl, fl
 }
 
 // Leaf of a mixed scene.  Returns true when an any-hit query is decided.
+// best_rec (optional): the record index of the best hit so far, for callers
+// that need the hit object's record afterwards (the G-buffer's normals).
 template <bool ANY, bool COUNT = false>
 __device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ prims, int32_t ref,
-                                                   const RayState& r, BestHit& best, uint32_t* pf = nullptr) {
+                                                   const RayState& r, BestHit& best, uint32_t* pf = nullptr,
+                                                   uint32_t* best_rec = nullptr) {
     uint32_t i = (uint32_t)~ref;
     for (;;) {
         const float4* p = prims + 3 * (size_t)i;
@@ -610,6 +619,8 @@ __device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ pr
                         best.v = v;
                         best.prim = prio_other(id);
                         best.tcull = cull_limit(t);
+                        if (best_rec)
+                            *best_rec = i;
                     }
                 }
             } else if (type == kPrimSphere) {
@@ -623,6 +634,8 @@ __device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ pr
                         best.t = t;
                         best.prim = prio_other(id);
                         best.tcull = cull_limit(t);
+                        if (best_rec)
+                            *best_rec = i;
                     }
                 }
             } else {
@@ -637,6 +650,8 @@ __device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ pr
                         best.v = v;
                         best.prim = prio_cube(id);
                         best.tcull = cull_limit(t);
+                        if (best_rec)
+                            *best_rec = i;
                     }
                 }
             }
@@ -649,9 +664,13 @@ __device__ __forceinline__ bool process_leaf_mixed(const float4* __restrict__ pr
 }
 
 // Planes of a mixed scene (outside the tree): every ray tests all of them.
+// best_rec (optional) receives kRecPlane | j when plane j becomes the best hit.
+constexpr uint32_t kRecPlane = 0x80000000u;
+
 template <bool ANY>
 __device__ __forceinline__ bool test_planes(const float4* __restrict__ planes, uint32_t count,
-                                            uint32_t base, const RayState& r, BestHit& best) {
+                                            uint32_t base, const RayState& r, BestHit& best,
+                                            uint32_t* best_rec = nullptr) {
     for (uint32_t j = 0; j < count; ++j) {
         const uint32_t id = base + j;
         if (id == r.prev)
@@ -668,6 +687,8 @@ __device__ __forceinline__ bool test_planes(const float4* __restrict__ planes, u
             best.t = t;
             best.prim = prio_other(id);
             best.tcull = cull_limit(t);
+            if (best_rec)
+                *best_rec = kRecPlane | j;
         }
     }
     return false;
@@ -701,6 +722,41 @@ __device__ __forceinline__ bool trace_single(const float4* __restrict__ nodes,
         next = st.pop_live(best.tcull);
         if (next == kRefDone)
             return false;
+    }
+}
+
+// Closest hit of one ray in a mixed scene by one thread, in the persistent
+// kernels' order: planes first, then the tree.  best.prim ends as a priority
+// code (id_of_prio gives the object) and best_rec as the best hit's record
+// index, or kRecPlane | plane index.
+template <int LAYOUT>
+__device__ __forceinline__ void trace_single_mixed(const float4* __restrict__ nodes,
+                                                   const float4* __restrict__ prims, uint32_t node_count,
+                                                   const float4* __restrict__ planes, uint32_t plane_count,
+                                                   uint32_t plane_base, const RayState& r, BestHit& best,
+                                                   TraversalStack& st, bool& overflow, uint32_t& best_rec) {
+    best.t = r.tmax_eff;
+    best.u = 0.f;
+    best.v = 0.f;
+    best.prim = kPrioNone;
+    best.tcull = cull_limit(best.t);
+    best_rec = 0xffffffffu;
+    if (plane_count)
+        test_planes<false>(planes, plane_count, plane_base, r, best, &best_rec);
+    if (!node_count)
+        return;
+    st.sp = 0;
+    uint32_t unused = 0;
+    int32_t next = 0;
+    for (;;) {
+        while (next >= 0 && next != kRefDone)
+            next = visit_node<LAYOUT, false, true>(nodes, next, r, best, st, overflow, unused);
+        if (next == kRefDone)
+            return;
+        process_leaf_mixed<false>(prims, next, r, best, nullptr, &best_rec);
+        next = st.pop_live(best.tcull);
+        if (next == kRefDone)
+            return;
     }
 }
 

@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define IGXRT_ABI_VERSION 2u
+#define IGXRT_ABI_VERSION 3u
 
 /* res/shaders/primitive.glsl:6-7: the miss distance and the "no object" id. */
 #define IGXRT_NO_HIT 3.4028235e38f
@@ -284,8 +284,9 @@ igxrt_status igxrt_scene_create(igxrt_context* ctx, const igxrt_triangle* tris,
  * needs t >= tmin, a plane hit t >= tmin, a cube hit only tmax >= tmin (a
  * cube around the origin is hit at its negative entry distance), and at equal
  * t a cube beats any other primitive and the later of two cubes wins (the
- * cube test rejects only tmin > hit.hitT).  The batched, shadow-mask and
- * G-buffer calls take triangle-only scenes. */
+ * cube test rejects only tmin > hit.hitT).  Every pass takes mixed scenes:
+ * batches, the server, the shadow mask and the G-buffer (whose object normal
+ * of a sphere, cube or plane is its geometry normal, trace.glsl:59-63). */
 igxrt_status igxrt_scene_create_mixed(igxrt_context* ctx, const igxrt_scene_desc* desc,
                                       const igxrt_build_options* opts, igxrt_scene** out);
 /* Uploads an already built BVH. */
@@ -490,10 +491,14 @@ typedef struct igxrt_server igxrt_server;
 typedef struct igxrt_server_options {
     uint64_t memory_cap_bytes;   /* device bytes for the ray, prev_hit and result
                                     buffers of admitted requests; 0 = 24 GiB */
-    uint32_t max_batch_rays;     /* rays coalesced into one launch, 0 = 4M */
-    uint32_t max_batch_requests; /* requests per launch, 0 = 1024 (at most 4096) */
+    uint32_t max_batch_rays;     /* rays coalesced into one launch, 0 = 1M */
+    uint32_t max_batch_requests; /* request slices per launch, 0 = 1024 (at most 4096) */
     uint32_t streams;            /* batches in flight at once, 0 = 2 */
-    uint32_t reserved[3];
+    uint32_t slice_rays;         /* a request enters a launch with at most this many
+                                    of its rays (the rest go into the next launches,
+                                    beside the requests queued behind it), so a large
+                                    request cannot hold small ones back; 0 = 256K */
+    uint32_t reserved[2];
 } igxrt_server_options;
 
 /* A ray-query request.  The arrays are host memory owned by the caller and
@@ -513,17 +518,19 @@ typedef struct igxrt_request {
 typedef struct igxrt_request_stats {
     double submitted;
     double admitted;  /* its buffers were reserved under the cap */
-    double launched;  /* its batch was queued on a stream */
-    double completed; /* its results were in host memory */
-    uint32_t batch;   /* sequence number of the launch that carried it */
+    double launched;  /* its first slice's batch was queued on a stream */
+    double completed; /* all its results were in host memory */
+    uint32_t batch;   /* sequence number of the launch that carried its last slice */
     uint32_t status;  /* igxrt_status of the request */
+    double arrival;   /* its scheduled arrival (igxrt_server_replay), else = submitted;
+                         latency is completed - arrival */
 } igxrt_request_stats;
 
 typedef struct igxrt_server_stats {
     uint64_t submitted, completed, rejected;
     uint64_t rays_completed;
     uint64_t batches;
-    double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> completed */
+    double p50_ms, p99_ms, mean_ms, max_ms; /* arrival -> completed */
     double first_submit, last_complete;     /* seconds since start */
     uint64_t peak_memory_bytes;             /* peak reserved under the cap */
     uint32_t peak_pending;                  /* most requests waiting for admission */
@@ -534,8 +541,8 @@ typedef struct igxrt_server_stats {
  * context must not be used by other threads while the server runs. */
 igxrt_status igxrt_server_create(igxrt_context* ctx, const igxrt_server_options* opts,
                                  igxrt_server** out);
-/* Registers a resident scene; it must outlive the server.  Mixed scenes, and
- * scenes without the server's node layout, are refused with
+/* Registers a resident scene (triangle-only or mixed); it must outlive the
+ * server.  Scenes without the server's node layout are refused with
  * IGXRT_ERROR_UNSUPPORTED. */
 igxrt_status igxrt_server_add_scene(igxrt_server* server, const igxrt_scene* scene,
                                     uint32_t* scene_id);
@@ -543,11 +550,35 @@ igxrt_status igxrt_server_add_scene(igxrt_server* server, const igxrt_scene* sce
  * fit the memory cap is refused with IGXRT_ERROR_ADMISSION; others wait in
  * FIFO order until their buffers fit. */
 igxrt_status igxrt_server_submit(igxrt_server* server, const igxrt_request* req, uint64_t* ticket);
+/* Submits `count` requests at scheduled times, pacing them natively on the
+ * calling thread: request i is submitted once arrival_s[i] seconds have passed
+ * since the call began (a sleep, then a spin for the last 200 us), and its
+ * latency is counted from that scheduled time, so a late submission counts
+ * against the server.  tickets[i] receives its ticket (0 when refused with
+ * IGXRT_ERROR_ADMISSION, which the call skips).  Returns after the last
+ * submission; the requests complete as usual. */
+igxrt_status igxrt_server_replay(igxrt_server* server, const igxrt_request* reqs,
+                                 const double* arrival_s, uint32_t count, uint64_t* tickets);
 /* Blocks until the request completes (IGXRT_ERROR_TIMEOUT after timeout_s,
  * < 0 = no limit); stats may be NULL. */
 igxrt_status igxrt_server_wait(igxrt_server* server, uint64_t ticket, double timeout_s,
                                igxrt_request_stats* stats);
 igxrt_status igxrt_server_get_stats(igxrt_server* server, igxrt_server_stats* stats);
+/* Device-side interval of one completed batch launch: the earliest CTA start
+ * and the latest warp exit of its kernel, read from %globaltimer by the kernel
+ * itself (nanoseconds, one clock for all streams), so intervals of batches on
+ * different streams show whether their kernels ran at the same time. */
+typedef struct igxrt_batch_time {
+    uint64_t start_ns;
+    uint64_t end_ns;
+    uint32_t batch;    /* sequence number, as igxrt_request_stats.batch */
+    uint32_t stream;   /* the server's stream slot it ran on */
+    uint64_t rays;
+} igxrt_batch_time;
+/* Copies the intervals of up to `max_batches` completed batches, in
+ * completion order, and sets *count to the number copied. */
+igxrt_status igxrt_server_batch_times(igxrt_server* server, igxrt_batch_time* times,
+                                      uint32_t max_batches, uint32_t* count);
 /* Finishes all queued work, then stops the scheduler and frees its memory. */
 igxrt_status igxrt_server_destroy(igxrt_server* server);
 

@@ -164,8 +164,13 @@ inline float max(float x, float y) { return x < y ? y : x; }
 inline float abs(float x) { return __builtin_fabsf(x); }
 inline float sign(float x) { return x > 0 ? 1.0f : (x < 0 ? -1.0f : 0.0f); }
 inline float sqrt(float x) { return __builtin_sqrtf(x); }
-inline float asin(float x) { return __builtin_asinf(x); }
-inline float atan(float y_over_x) { return __builtin_atanf(y_over_x); }
+/* asin and atan: the GLSL specification leaves their precision to the
+ * implementation.  They are fixed here as the correctly rounded binary32
+ * values, evaluated in binary64 and rounded once (a host libm's binary32
+ * asinf / atanf are not correctly rounded and differ between libraries), so
+ * the sphere uv of primitive.glsl:198-204 has one exact answer. */
+inline float asin(float x) { return (float)__builtin_asin((double)x); }
+inline float atan(float y_over_x) { return (float)__builtin_atan((double)y_over_x); }
 inline bool isnan(float x) { return x != x; }
 
 /* ---- geometric builtins --------------------------------------------------- */

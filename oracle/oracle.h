@@ -104,6 +104,30 @@ void orc_trace_occlusion_mixed(const igxrt_scene_desc* scene, const igxrt_ray* r
                                const uint32_t* prev_hit, uint32_t nrays, uint32_t* out,
                                uint32_t* flags, int threads);
 
+/*
+ * The oracle's own BVH over `ntri` triangles (bvh_build_oracle.c: binned SAH,
+ * leaves of at most 4 triangles, boxes padded outward) in the BVH2 node and
+ * primitive-record formats orc_bvh_trace reads, so the CPU reference arm
+ * traces without the engine's builder.  nodes must hold max(1, ntri) nodes and
+ * prims ntri records.  Returns the node count (0 for no triangles), or -1 when
+ * memory runs out.
+ */
+int64_t orc_bvh_build(const igxrt_triangle* tris, uint32_t ntri, igxrt_bvh2_node* nodes,
+                      igxrt_prim_record* prims);
+
+/* The primary rays orc_gbuffer traces, width*height records in pixel order
+ * ({eye, 0, dir, IGXRT_NO_HIT}). */
+void orc_camera_rays(const igxrt_camera* cam, igxrt_ray* rays);
+
+/* orc_gbuffer / orc_shadow_mask over every primitive buffer of a mixed scene
+ * (trace.glsl:22-46 order).  The G-buffer's object normal of a sphere, cube
+ * or plane hit is its geometry normal (trace.glsl:59-63). */
+void orc_gbuffer_mixed(const igxrt_scene_desc* scene, const igxrt_camera* cam, float* dir_object,
+                       float* uv_normal, uint32_t* flags, int threads);
+void orc_shadow_mask_mixed(const igxrt_scene_desc* scene, const igxrt_ray* rays, const uint32_t* object,
+                           uint32_t width, uint32_t height, uint32_t samples, uint32_t* mask,
+                           uint32_t* flags, int threads);
+
 /* Number of hardware threads the oracle uses for threads <= 0. */
 int orc_hardware_threads(void);
 

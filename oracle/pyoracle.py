@@ -21,7 +21,9 @@ ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(ORACLE_DIR, "liboracle.so")
 REF_LIB = os.path.join(ORACLE_DIR, "_ref", "libigxref.so")
 REF_GEN = os.path.join(ORACLE_DIR, "_ref", "gen")
-REFERENCE_CHECKOUT = "/root/reference"
+# The reference checkout, needed only to (re)generate _ref/: taken from the
+# IGXRT_REFERENCE environment variable (no default location).
+REFERENCE_ENV = "IGXRT_REFERENCE"
 
 EVENT_NAN_T = 1
 EVENT_ZERO_DET = 2
@@ -33,12 +35,19 @@ REF_HIT_DTYPE = np.dtype([("rayDir", "<f4", (3,)), ("hitT", "<f4"), ("uv", "<f4"
                           ("objectNormal", "<f4", (3,))])
 
 
-def build(with_reference: bool = True) -> None:
-    """Builds liboracle.so, and _ref/libigxref.so when its sources are available."""
+def build(with_reference: bool = True, reference: str | None = None) -> None:
+    """Builds liboracle.so, and _ref/libigxref.so when its sources are
+    available: the reference checkout `reference` (default: the
+    IGXRT_REFERENCE environment variable), or an _ref/gen/ left by an earlier
+    build."""
     subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
-    have_checkout = os.path.exists(os.path.join(REFERENCE_CHECKOUT, "res", "shaders", "trace.glsl"))
+    reference = reference or os.environ.get(REFERENCE_ENV) or ""
+    have_checkout = bool(reference) and os.path.exists(os.path.join(reference, "res", "shaders", "trace.glsl"))
     if with_reference and (have_checkout or os.path.isdir(REF_GEN)):
-        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref"], check=True)
+        cmd = ["make", "-s", "-C", ORACLE_DIR, "ref"]
+        if have_checkout:
+            cmd.append(f"REF={reference}")
+        subprocess.run(cmd, check=True)
 
 
 _lib = None
@@ -72,6 +81,14 @@ def lib() -> C.CDLL:
         h.orc_trace_geometry_mixed.restype = None
         h.orc_trace_occlusion_mixed.argtypes = [vp, vp, vp, u32, vp, vp, i32]
         h.orc_trace_occlusion_mixed.restype = None
+        h.orc_camera_rays.argtypes = [vp, vp]
+        h.orc_camera_rays.restype = None
+        h.orc_gbuffer_mixed.argtypes = [vp, vp, vp, vp, vp, i32]
+        h.orc_gbuffer_mixed.restype = None
+        h.orc_shadow_mask_mixed.argtypes = [vp, vp, vp, u32, u32, u32, vp, vp, i32]
+        h.orc_shadow_mask_mixed.restype = None
+        h.orc_bvh_build.argtypes = [vp, u32, vp, vp]
+        h.orc_bvh_build.restype = C.c_int64
         h.orc_hardware_threads.argtypes = []
         h.orc_hardware_threads.restype = i32
         _lib = h
@@ -253,6 +270,43 @@ def trace_occlusion_mixed(rays, prev=None, tris=None, spheres=None, cubes=None, 
     return out, flags
 
 
+def camera_rays(camera: np.ndarray) -> np.ndarray:
+    """The oracle's primary rays of a camera (calculateScreen), pixel order."""
+    cam = np.ascontiguousarray(camera, dtype=CAMERA_DTYPE).reshape(1)
+    rays = np.zeros(int(cam["width"][0]) * int(cam["height"][0]), dtype=RAY_DTYPE)
+    lib().orc_camera_rays(_ptr(cam), _ptr(rays))
+    return rays
+
+
+def gbuffer_mixed(camera: np.ndarray, tris=None, spheres=None, cubes=None, planes=None,
+                  threads: int = 0, uv_fill: float = 0.0):
+    """The reference's primary pass over a mixed scene (brute force):
+    (dir_object, uv_normal, flags) as gbuffer()."""
+    d, keep = scene_desc(tris, spheres, cubes, planes)
+    cam = np.ascontiguousarray(camera, dtype=CAMERA_DTYPE).reshape(1)
+    w, h = int(cam["width"][0]), int(cam["height"][0])
+    do = np.zeros((h, w, 4), dtype=np.float32)
+    uv = np.full((h, w, 4), uv_fill, dtype=np.float32)
+    flags = np.zeros(w * h, dtype=np.uint32)
+    lib().orc_gbuffer_mixed(C.addressof(d), _ptr(cam), _ptr(do), _ptr(uv), _ptr(flags), threads)
+    return do, uv, flags
+
+
+def shadow_mask_mixed(rays, object_, width: int, height: int, samples: int, tris=None, spheres=None,
+                      cubes=None, planes=None, threads: int = 0):
+    """The reference's shadow pass over a mixed scene, packed as shadow_mask()."""
+    d, keep = scene_desc(tris, spheres, cubes, planes)
+    rays = np.ascontiguousarray(rays)
+    obj = np.ascontiguousarray(object_, dtype=np.uint32)
+    assert len(rays) == width * height * samples and len(obj) == width * height
+    words = ((width + 15) // 16) * ((height + 1) // 2) * samples
+    mask = np.zeros(words, dtype=np.uint32)
+    flags = np.zeros(len(rays), dtype=np.uint32)
+    lib().orc_shadow_mask_mixed(C.addressof(d), _ptr(rays), _ptr(obj), width, height, samples,
+                                _ptr(mask), _ptr(flags), threads)
+    return mask, flags
+
+
 def reintersect_f64(ray: np.ndarray, tri: np.ndarray):
     t, u, v = C.c_double(), C.c_double(), C.c_double()
     r = np.ascontiguousarray(ray)
@@ -280,6 +334,27 @@ def bvh_trace(layout: int, nodes: np.ndarray, prims: np.ndarray, rays: np.ndarra
         raise RuntimeError("oracle BVH traversal met a malformed BVH")
     res = hits if mode == 0 else occ
     return (res, nf, pf) if counts else res
+
+
+BVH2_NODE_DTYPE = np.dtype([("c0_x", "<f4", (2,)), ("c0_y", "<f4", (2,)), ("c1_x", "<f4", (2,)),
+                            ("c1_y", "<f4", (2,)), ("c0_z", "<f4", (2,)), ("c1_z", "<f4", (2,)),
+                            ("child", "<i4", (2,)), ("pad", "<u4", (2,))])
+PRIM_RECORD_DTYPE = np.dtype([("p0", "<f4", (3,)), ("prim", "<u4"), ("e1", "<f4", (3,)),
+                              ("leaf_end", "<u4"), ("e2", "<f4", (3,)), ("pad", "<u4")])
+
+
+def bvh_build(tris: np.ndarray):
+    """The oracle's own binned-SAH BVH2 (bvh_build_oracle.c) over `tris`:
+    (nodes, prims) in the arrays bvh_trace(0, ...) reads.  Used by the CPU
+    reference arm, which must not run the engine's builder."""
+    tris = np.ascontiguousarray(tris)
+    n = len(tris)
+    nodes = np.zeros(max(1, n), dtype=BVH2_NODE_DTYPE)
+    prims = np.zeros(n, dtype=PRIM_RECORD_DTYPE)
+    count = lib().orc_bvh_build(_ptr(tris), n, _ptr(nodes), _ptr(prims)) if n else 0
+    if count < 0:
+        raise MemoryError("oracle BVH build ran out of memory")
+    return nodes[:count], prims
 
 
 # --- the reference's own shader code --------------------------------------

@@ -60,6 +60,8 @@ typedef struct {
     float u, v;
     uint32_t object;
     uint32_t events;
+    float gn[3]; /* hit.geometryNormal of a sphere, cube or plane hit (the
+                    G-buffer's object normal for those, trace.glsl:59-63) */
 } hitstate;
 
 /*
@@ -299,8 +301,12 @@ static int ray_intersect_sphere(v3 pos, v3 dir, float tmin, const float* sphere,
         hit->hitT = hitT;
         const v3 o = add(scale(dir, hitT), pos);          /* :189 */
         const v3 normal = normalize3(sub(c, o));          /* :190 */
-        const float latitude = asinf(normal.z);           /* :198 */
-        float longitude = atanf(normal.y / normal.x);     /* :199 */
+        hit->gn[0] = normal.x;                            /* :192 */
+        hit->gn[1] = normal.y;
+        hit->gn[2] = normal.z;
+        /* asin / atan correctly rounded to binary32 (binary64, rounded once) */
+        const float latitude = (float)asin((double)normal.z);            /* :198 */
+        float longitude = (float)atan((double)(normal.y / normal.x));    /* :199 */
         if (longitude != longitude)                       /* :201-202 */
             longitude = 0;
         const float k = (float)(0.636619746685 * 0.5);    /* :204 */
@@ -321,6 +327,10 @@ static int ray_intersect_plane(v3 pos, v3 dir, float tmin, const float* plane, u
     const float hitT = -(dot(pos, neg) + plane[3]) / dif; /* :219 */
     if (hitT >= tmin && obj != prevObj && hitT < hit->hitT) { /* :221 */
         hit->hitT = hitT;
+        const v3 gn = dif > 0 ? neg : pdir;             /* :224 */
+        hit->gn[0] = gn.x;
+        hit->gn[1] = gn.y;
+        hit->gn[2] = gn.z;
         const v3 o = add(scale(dir, hitT), pos);        /* :226 */
         const v3 z = {0, 0, 1}, x = {1, 0, 0};
         const v3 planeX = cross(n, z);                  /* :228 */
@@ -351,13 +361,17 @@ static int ray_intersect_cube(v3 pos, v3 dir, float tmin_ray, const igxrt_cube* 
     p.x = p.x / end.x;                                  /* :309 */
     p.y = p.y / end.y;
     p.z = p.z / end.z;
+    hit->gn[0] = hit->gn[1] = hit->gn[2] = 0;
     if (tmin == mi.x) {                                 /* :311-327 */
+        hit->gn[0] = mi.x == startDir.x ? 1.0f : -1.0f; /* isLeft * 2 - 1 */
         hit->u = p.y;
         hit->v = p.z;
     } else if (tmin == mi.y) {
+        hit->gn[1] = mi.y == startDir.y ? 1.0f : -1.0f; /* isDown * 2 - 1 */
         hit->u = p.x;
         hit->v = p.z;
     } else {
+        hit->gn[2] = mi.z == startDir.z ? 1.0f : -1.0f; /* isBack * 2 - 1 */
         hit->u = p.x;
         hit->v = p.y;
     }
@@ -516,34 +530,64 @@ typedef struct {
     float* dir_object;
     float* uv_normal;
     uint32_t* flags;
+    const igxrt_scene_desc* scene; /* non-NULL: every primitive type (mixed scenes) */
 } gbuffer_ctx;
+
+/* The primary ray of pixel (x, y): calculatePrimary (camera.glsl:115-116)
+ * and calculateScreen (:72-87), origin at the eye. */
+static void camera_ray(const igxrt_camera* c, float inv_w, float inv_h, uint32_t x, uint32_t y,
+                       igxrt_ray* ray) {
+    const float cx = ((float)x + c->jitter_x) * inv_w;
+    const float cy = 1 - ((float)y + c->jitter_y) * inv_h;
+    float d[3];
+    for (int k = 0; k < 3; ++k) {
+        const float right = c->p1[k] - c->p0[k], up = c->p2[k] - c->p0[k];
+        const float pos = c->p0[k] + cx * right + cy * up;
+        d[k] = pos - c->eye[k];
+    }
+    const v3 dv = {d[0], d[1], d[2]};
+    const float len = sqrtf(dot(dv, dv));
+    for (int k = 0; k < 3; ++k) {
+        ray->org[k] = c->eye[k];
+        ray->dir[k] = d[k] / len;
+    }
+    ray->tmin = 0.0f;
+    ray->tmax = IGXRT_NO_HIT;
+}
+
+void orc_camera_rays(const igxrt_camera* cam, igxrt_ray* rays) {
+    const float inv_w = 1.0f / (float)cam->width, inv_h = 1.0f / (float)cam->height;
+    for (uint32_t y = 0; y < cam->height; ++y)
+        for (uint32_t x = 0; x < cam->width; ++x)
+            camera_ray(cam, inv_w, inv_h, x, y, &rays[(size_t)y * cam->width + x]);
+}
 
 static void gbuffer_chunk(void* p, uint32_t b, uint32_t e) {
     gbuffer_ctx* g = (gbuffer_ctx*)p;
     const igxrt_camera* c = g->cam;
     for (uint32_t i = b; i < e; ++i) {
-        const uint32_t x = i % c->width, y = i / c->width;
-        /* calculatePrimary (camera.glsl:115-116) and calculateScreen (:72-87) */
-        const float cx = ((float)x + c->jitter_x) * g->inv_w;
-        const float cy = 1 - ((float)y + c->jitter_y) * g->inv_h;
-        float d[3];
-        for (int k = 0; k < 3; ++k) {
-            const float right = c->p1[k] - c->p0[k], up = c->p2[k] - c->p0[k];
-            const float pos = c->p0[k] + cx * right + cy * up;
-            d[k] = pos - c->eye[k];
-        }
-        const v3 dv = {d[0], d[1], d[2]};
-        const float len = sqrtf(dot(dv, dv));
         igxrt_ray ray;
-        for (int k = 0; k < 3; ++k) {
-            ray.org[k] = c->eye[k];
-            ray.dir[k] = d[k] / len;
-        }
-        ray.tmin = 0.0f;
-        ray.tmax = IGXRT_NO_HIT;
+        camera_ray(c, g->inv_w, g->inv_h, i % c->width, i / c->width, &ray);
         igxrt_hit h;
         uint32_t f = 0;
-        trace_geometry_one(g->tris, g->ntri, &ray, IGXRT_NO_RAY_HIT, &h, &f);
+        float gn[3] = {0, 0, 0};
+        if (g->scene) {
+            hitstate hs;
+            hs.hitT = IGXRT_NO_HIT;
+            hs.u = hs.v = 0;
+            hs.object = 0;
+            hs.events = 0;
+            trace_mixed_one(g->scene, &ray, IGXRT_NO_RAY_HIT, &hs);
+            f = hs.events;
+            /* raygen.comp:40: a miss is hitT == noHit */
+            h.t = hs.hitT;
+            h.u = hs.u;
+            h.v = hs.v;
+            h.prim = hs.hitT == IGXRT_NO_HIT ? IGXRT_NO_RAY_HIT : hs.object;
+            memcpy(gn, hs.gn, sizeof(gn));
+        } else {
+            trace_geometry_one(g->tris, g->ntri, &ray, IGXRT_NO_RAY_HIT, &h, &f);
+        }
         if (g->flags)
             g->flags[i] = f;
         float* dob = g->dir_object + 4 * (size_t)i;
@@ -552,15 +596,21 @@ static void gbuffer_chunk(void* p, uint32_t b, uint32_t e) {
             for (int k = 0; k < 3; ++k)
                 dob[k] = ray.dir[k] * h.t;
             memcpy(&dob[3], &h.prim, 4);
-            /* trace.glsl:50-57, raygen.comp:46-51 */
-            const igxrt_triangle* t = &g->tris[h.prim];
-            float n0[3], n1[3], n2[3], n[3];
-            orc_decode_spheremap(t->n0, n0);
-            orc_decode_spheremap(t->n1, n1);
-            orc_decode_spheremap(t->n2, n2);
-            const float bw = 1 - h.u - h.v; /* interpolate, primitive.glsl:146-151 */
-            for (int k = 0; k < 3; ++k)
-                n[k] = h.u * n1[k] + h.v * n2[k] + bw * n0[k];
+            /* trace.glsl:50-63, raygen.comp:46-51: a triangle's interpolated
+             * vertex normal, any other object's geometry normal */
+            float n[3];
+            if (h.prim < g->ntri) {
+                const igxrt_triangle* t = &g->tris[h.prim];
+                float n0[3], n1[3], n2[3];
+                orc_decode_spheremap(t->n0, n0);
+                orc_decode_spheremap(t->n1, n1);
+                orc_decode_spheremap(t->n2, n2);
+                const float bw = 1 - h.u - h.v; /* interpolate, primitive.glsl:146-151 */
+                for (int k = 0; k < 3; ++k)
+                    n[k] = h.u * n1[k] + h.v * n2[k] + bw * n0[k];
+            } else {
+                memcpy(n, gn, sizeof(n));
+            }
             uint32_t enc[2];
             orc_encode_normal(n, enc);
             float* uvn = g->uv_normal + 4 * (size_t)i;
@@ -580,7 +630,14 @@ static void gbuffer_chunk(void* p, uint32_t b, uint32_t e) {
 void orc_gbuffer(const igxrt_triangle* tris, uint32_t ntri, const igxrt_camera* cam,
                  float* dir_object, float* uv_normal, uint32_t* flags, int threads) {
     gbuffer_ctx g = {tris, ntri, cam, 1.0f / (float)cam->width, 1.0f / (float)cam->height,
-                     dir_object, uv_normal, flags};
+                     dir_object, uv_normal, flags, NULL};
+    run_parallel(gbuffer_chunk, &g, cam->width * cam->height, 64, threads);
+}
+
+void orc_gbuffer_mixed(const igxrt_scene_desc* scene, const igxrt_camera* cam, float* dir_object,
+                       float* uv_normal, uint32_t* flags, int threads) {
+    gbuffer_ctx g = {scene->triangles, scene->triangle_count, cam, 1.0f / (float)cam->width,
+                     1.0f / (float)cam->height, dir_object, uv_normal, flags, scene};
     run_parallel(gbuffer_chunk, &g, cam->width * cam->height, 64, threads);
 }
 
@@ -602,6 +659,7 @@ typedef struct {
     uint32_t w, h;
     uint32_t* occ;
     uint32_t* flags;
+    const igxrt_scene_desc* scene; /* non-NULL: every primitive type (mixed scenes) */
 } shadow_ctx;
 
 static void shadow_chunk(void* p, uint32_t b, uint32_t e) {
@@ -611,19 +669,50 @@ static void shadow_chunk(void* p, uint32_t b, uint32_t e) {
         const uint32_t obj = c->object[pix];
         uint32_t f = 0;
         c->occ[i] = 0;
-        if (obj != IGXRT_NO_RAY_HIT) /* nv_all.shadow.comp:108 */
-            trace_occlusion_one(c->tris, c->ntri, &c->rays[i], obj, &c->occ[i], &f);
+        if (obj != IGXRT_NO_RAY_HIT) { /* nv_all.shadow.comp:108 */
+            if (c->scene) {
+                hitstate hs;
+                hs.hitT = IGXRT_NO_HIT;
+                hs.u = hs.v = 0;
+                hs.object = 0;
+                hs.events = 0;
+                trace_mixed_one(c->scene, &c->rays[i], obj, &hs);
+                c->occ[i] = hs.hitT < tmax_effective(c->rays[i].tmax) ? 1u : 0u; /* trace.glsl:97 */
+                f = hs.events;
+            } else {
+                trace_occlusion_one(c->tris, c->ntri, &c->rays[i], obj, &c->occ[i], &f);
+            }
+        }
         if (c->flags)
             c->flags[i] = f;
     }
 }
 
+static void shadow_mask_impl(const igxrt_triangle* tris, uint32_t ntri, const igxrt_scene_desc* scene,
+                             const igxrt_ray* rays, const uint32_t* object, uint32_t width,
+                             uint32_t height, uint32_t samples, uint32_t* mask, uint32_t* flags,
+                             int threads);
+
 void orc_shadow_mask(const igxrt_triangle* tris, uint32_t ntri, const igxrt_ray* rays,
                      const uint32_t* object, uint32_t width, uint32_t height, uint32_t samples,
                      uint32_t* mask, uint32_t* flags, int threads) {
+    shadow_mask_impl(tris, ntri, NULL, rays, object, width, height, samples, mask, flags, threads);
+}
+
+void orc_shadow_mask_mixed(const igxrt_scene_desc* scene, const igxrt_ray* rays, const uint32_t* object,
+                           uint32_t width, uint32_t height, uint32_t samples, uint32_t* mask,
+                           uint32_t* flags, int threads) {
+    shadow_mask_impl(scene->triangles, scene->triangle_count, scene, rays, object, width, height, samples,
+                     mask, flags, threads);
+}
+
+static void shadow_mask_impl(const igxrt_triangle* tris, uint32_t ntri, const igxrt_scene_desc* scene,
+                             const igxrt_ray* rays, const uint32_t* object, uint32_t width,
+                             uint32_t height, uint32_t samples, uint32_t* mask, uint32_t* flags,
+                             int threads) {
     const uint32_t n = width * height * samples;
     uint32_t* occ = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
-    shadow_ctx c = {tris, ntri, rays, object, width, height, occ, flags};
+    shadow_ctx c = {tris, ntri, rays, object, width, height, occ, flags, scene};
     run_parallel(shadow_chunk, &c, n, 64, threads);
     const uint32_t tiles_x = (width + 15) / 16, tiles_y = (height + 1) / 2;
     memset(mask, 0, sizeof(uint32_t) * (size_t)tiles_x * tiles_y * samples);

@@ -7,7 +7,9 @@ res/shaders/primitive.glsl and trace.glsl compiled for the host
 checkout, so this script runs where the checkout is; the .npz files it writes
 are committed and checked everywhere.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [REFERENCE_CHECKOUT]
+
+(the checkout defaults to the IGXRT_REFERENCE environment variable).
 """
 from __future__ import annotations
 
@@ -120,7 +122,7 @@ def niels_mixed():
 
 
 def main() -> None:
-    pyoracle.build(with_reference=True)
+    pyoracle.build(with_reference=True, reference=sys.argv[1] if len(sys.argv) > 1 else None)
     if not pyoracle.have_reference():
         raise SystemExit("oracle/_ref/libigxref.so is not built: the reference checkout is needed")
 
@@ -165,6 +167,28 @@ def main() -> None:
                         hit_object=h["object"], geometry_normal=h["geometryNormal"],
                         object_normal=h["objectNormal"])
     print(f"niels_mixed: {len(r)} rays, {int((h['hitT'] < NO_HIT).sum())} hits")
+
+    # 4b. the primary pass over the mixed scene: raygen.comp's two images
+    #     (:39-51) from the reference's traceGeometry on the camera's rays
+    #     (trace.glsl:48-63: an interpolated vertex normal for triangles, the
+    #     geometry normal for spheres, cubes and planes)
+    cam = scenes.camera_record(96, 64, eye=(7.0, 11.0, 6.0), target=(0.0, 2.5, 0.0), vfov_deg=70.0)
+    crays = pyoracle.camera_rays(cam)
+    h = pyoracle.ref_trace_geometry(t, rays6(crays), None, spheres=s, cubes=c, planes=pl)
+    hit = h["hitT"] != NO_HIT
+    d = crays["dir"].astype(np.float32)
+    do = np.zeros((len(crays), 4), np.float32)
+    do[:, :3] = np.where(hit[:, None], d * h["hitT"][:, None].astype(np.float32), d)
+    do[:, 3] = np.where(hit, h["object"], np.uint32(0xFFFFFFFF)).astype(np.uint32).view(np.float32)
+    uvn = np.zeros((len(crays), 4), np.float32)
+    enc = pyoracle.ref_encode_normal(h["objectNormal"])
+    uvn[:, :2] = np.where(hit[:, None], h["uv"], 0.0)
+    uvn[:, 2:] = np.where(hit[:, None], enc, 0).astype(np.uint32).view(np.float32)
+    np.savez_compressed(os.path.join(HERE, "niels_gbuffer.npz"), tris=t, spheres=s, cubes=c, planes=pl,
+                        camera=cam, dir_object=do.reshape(64, 96, 4), uv_normal=uvn.reshape(64, 96, 4))
+    kinds = np.searchsorted([len(t), len(t) + len(s), len(t) + len(s) + len(c)], h["object"][hit], "right")
+    print(f"niels_gbuffer: {int(hit.sum())} hits of {len(crays)} pixels, per kind "
+          f"{np.bincount(kinds, minlength=4).tolist()} (triangle, sphere, cube, plane)")
 
     # 5. packed vertex normals: decodeSpheremap, interpolate and encodeNormal
     rng2 = np.random.default_rng(scenes.seed_for(9, 1))

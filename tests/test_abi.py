@@ -94,7 +94,8 @@ _STRUCTS = {"BuildOptions": "igxrt_build_options", "BvhInfo": "igxrt_bvh_info",
             "LaunchParams": "igxrt_launch_params", "BatchItem": "igxrt_batch_item",
             "TuneOptions": "igxrt_tune_options", "ServerOptions": "igxrt_server_options",
             "Request": "igxrt_request", "RequestStats": "igxrt_request_stats",
-            "ServerStats": "igxrt_server_stats", "SceneDesc": "igxrt_scene_desc"}
+            "ServerStats": "igxrt_server_stats", "SceneDesc": "igxrt_scene_desc",
+            "BatchTime": "igxrt_batch_time"}
 _RECORDS = {"TRIANGLE_DTYPE": "igxrt_triangle", "RAY_DTYPE": "igxrt_ray", "HIT_DTYPE": "igxrt_hit",
             "PRIM_RECORD_DTYPE": "igxrt_prim_record", "BVH2_NODE_DTYPE": "igxrt_bvh2_node",
             "BVH4_NODE_DTYPE": "igxrt_bvh4_node", "BVH8_NODE_DTYPE": "igxrt_bvh8_node",

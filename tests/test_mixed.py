@@ -1,11 +1,13 @@
 """Scenes with spheres, cubes and planes (the reference's other primitive
 types, primitive.glsl:173-333, in the global order of trace.glsl:22-46).
 
-Tolerance: object ids and t bit-exact; u, v bit-exact except on sphere hits,
-whose uv is asin/atan(..) * 0.3183.. + 0.5 (primitive.glsl:198-204) with
-CUDA's asinf/atanf against the host C library's.  Both stay within 2 ulp of
-values below pi/2 (2.4e-7); scaled and shifted that bounds |du|, |dv| by
-2^-21 absolute (an ulp count is meaningless where u cancels towards 0)."""
+Tolerance: object ids and t bit-exact; u, v within 2 ulp (the tolerance of
+the traversal's floating-point outputs), and bit-exact in practice.  A sphere
+hit's uv is asin/atan(..) * 0.3183.. + 0.5 (primitive.glsl:198-204), which
+cancels towards 0 near the poles and the seam, so one ulp of difference in
+asin or atan would show as many ulp of u; the engine and the oracle both
+evaluate asin and atan correctly rounded (binary64, rounded once to
+binary32), which leaves them no room to differ."""
 import math
 import os
 
@@ -17,7 +19,7 @@ from igx_raytracing_gb300 import BVH, IgxrtError, scenes
 from igx_raytracing_gb300._capi import CUBE_DTYPE, RAY_DTYPE
 from oracle import pyoracle
 
-SPHERE_UV_ABS = 2.0 ** -21
+UV_ULPS = 2
 
 
 def golden_scene():
@@ -42,8 +44,8 @@ def assert_mixed_equal(got, prim, t, u, v, n_tris, n_spheres):
     for f, e in (("u", u), ("v", v)):
         assert np.array_equal(bits(got[f])[other], bits(e)[other])
         if sphere.any():
-            diff = np.abs(got[f][sphere].astype(np.float64) - e[sphere].astype(np.float64))
-            assert diff.max() <= SPHERE_UV_ABS, (diff.max(), ulp_diff(got[f][sphere], e[sphere]).max())
+            d = ulp_diff(got[f][sphere], e[sphere])
+            assert d.max() <= UV_ULPS, (f, int(d.max()), int((d > 0).sum()))
 
 
 def random_mixed(seed, nt=3000, ns=400, nc=300, npl=2):
@@ -157,15 +159,12 @@ def test_gpu_mixed_matches_oracle(ctx, layout, seed):
 
 
 @pytest.mark.gpu
-def test_mixed_scene_counts_and_unsupported_passes(ctx):
+def test_mixed_scene_fetch_counts(ctx):
+    # the G-buffer, shadow, batch and server passes over mixed scenes are
+    # checked against the oracle in test_mixed_passes.py
     sc = random_mixed(5, nt=100, ns=10, nc=10, npl=1)
     scene = ctx.create_scene_mixed(sc["tris"], sc["spheres"], sc["cubes"], sc["planes"])
     rays = mixed_rays(5, 64)
     nf, pf = ctx.count_fetches(scene, rays)  # GPU-side counts (no host traversal of typed leaves)
     hit = scene.trace_geometry(rays)["prim"] < 120
     assert (nf[hit] >= 1).all() and (pf[hit] >= 1).all()
-    cam = scenes.camera_record(8, 8, eye=(0.5, -1, 0.5), target=(0.5, 0.5, 0.5))
-    with pytest.raises(IgxrtError):
-        ctx.trace_gbuffer(scene, cam)
-    with pytest.raises(IgxrtError):
-        ctx.trace_shadow_mask(scene, rays, np.zeros(64, np.uint32), 8, 8, 1)

@@ -1,0 +1,187 @@
+"""Parity at the benchmark's full sizes (GPU): every ray of the 1M-triangle
+sphere step, of 4M incoherent rays over 1M and 2M random triangles, of the
+64-scene batch and of a sample of served requests, against the oracle.
+
+Each GPU result is compared bit for bit (prim, t, u, v; occlusion words):
+  - on every ray, with the oracle's CPU traversal of the engine's own tree
+    and of a tree the oracle builds itself (oracle/bvh_build_oracle.c), so
+    neither the engine's builder nor its visiting order is trusted;
+  - on a seeded subset of 16,384 rays per batch (4,096 per batch item, 256
+    per served request), with the brute-force loop over every triangle that
+    restates the reference (trace.glsl:9-98 around primitive.glsl:239-284);
+    rays on which that loop accepts a NaN t (an index-order artefact no BVH
+    reproduces) are left out of that comparison only, and there are none in
+    these generators' scenes.
+Disagreements are re-intersected in binary64 and printed (conftest.f64_report).
+The sphere's bounce and shadow rays start at its primary hits once those
+have been checked against the oracle."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import assert_hits_equal
+from igx_raytracing_gb300 import BVH, scenes
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+SUBSET = 16384
+
+
+def _subset(n, k, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, size=min(n, k), replace=False))
+
+
+def _check(tris, rays, prev, mode, got, bvh, oracle_tree, what, subset=SUBSET, seed=0):
+    """got (the engine's results for every ray) against the oracle: CPU
+    traversal of the engine's tree and of the oracle's tree on every ray, the
+    brute-force loop on a seeded subset (none when subset is 0)."""
+    nodes, prims = bvh.arrays(0)
+    trees = [("engine tree", nodes, prims), ("oracle tree", *oracle_tree)]
+    for name, nd, pr in trees:
+        e = pyoracle.bvh_trace(0, nd, pr, rays, prev, mode=mode)
+        if mode == 0:
+            assert_hits_equal(got, e["prim"], e["t"], e["u"], e["v"], f"{what}, {name}", rays, tris)
+        else:
+            bad = np.nonzero(got != e)[0]
+            assert len(bad) == 0, f"{what}, {name}: {len(bad)} occlusion words differ, first {bad[:8]}"
+    if subset == 0:
+        return
+    idx = _subset(len(rays), subset, seed)
+    r = rays[idx]
+    p = None if prev is None else prev[idx]
+    if mode == 0:
+        e, flags = pyoracle.trace_geometry(tris, r, p)
+        ok = (flags & pyoracle.EVENT_NAN_T) == 0
+        assert ok.all(), f"{what}: {int((~ok).sum())} rays with a NaN-t event"
+        assert_hits_equal(got[idx], e["prim"], e["t"], e["u"], e["v"], f"{what}, brute force", r, tris)
+    else:
+        e, flags = pyoracle.trace_occlusion(tris, r, p)
+        assert not (flags & pyoracle.EVENT_NAN_T).any()
+        assert np.array_equal(got[idx], e), f"{what}: brute-force occlusion differs"
+
+
+@pytest.fixture(scope="module")
+def sphere():
+    tris, prim = scenes.workload_sphere_primary()
+    bvh = BVH.build(tris)
+    return tris, prim, bvh, pyoracle.bvh_build(tris)
+
+
+def test_sphere_step_full_size(ctx, sphere):
+    """Config 2: 1,048,576 triangles; 2,073,600 primaries, then one bounce
+    and one shadow ray per primary hit (prev_hit = the hit)."""
+    tris, prim, bvh, otree = sphere
+    scene = ctx.create_scene(bvh=bvh)
+    hits = scene.trace_geometry(prim)
+    _check(tris, prim, None, 0, hits, bvh, otree, "sphere primaries", seed=1)
+    # the primary hits are now the oracle's: the secondaries start there
+    bounce, shadow, prev = scenes.secondary_rays(tris, prim, hits, scenes.SPHERE_LIGHT, scenes.seed_for(2, 50))
+    assert len(bounce) > 300000
+    got_b = scene.trace_geometry(bounce, prev)
+    _check(tris, bounce, prev, 0, got_b, bvh, otree, "sphere bounce", seed=2)
+    got_s = scene.trace_occlusion(shadow, prev)
+    _check(tris, shadow, prev, 1, got_s, bvh, otree, "sphere shadow", seed=3)
+    assert got_s.any() and not got_s.all()
+    scene.close()
+
+
+@pytest.mark.parametrize("ntris,variant", [(1_048_576, 1), (2_097_152, 0)])
+def test_incoherent_full_size(ctx, ntris, variant):
+    """Config 3 (2M triangles) and its 1M variant: 4,194,304 incoherent rays."""
+    tris, rays = scenes.workload_incoherent(ntris, 4_194_304, variant=variant)
+    bvh = BVH.build(tris)
+    otree = pyoracle.bvh_build(tris)
+    scene = ctx.create_scene(bvh=bvh)
+    for layout in (0, 1):
+        saved = ctx.launch_params
+        ctx.set_launch_params(layout=layout)
+        try:
+            got = scene.trace_geometry(rays)
+        finally:
+            ctx.set_launch_params(**saved)
+        # the brute-force subset once; every ray in both layouts
+        _check(tris, rays, None, 0, got, bvh, otree, f"incoherent {ntris}, layout {layout}",
+               subset=SUBSET if layout == 0 else 0, seed=4 + variant)
+    scene.close()
+
+
+def test_batch_64_scenes_full_size(ctx):
+    """Config 4: the 64-scene batch (1K-512K triangles, 4K-2M rays per item,
+    20.6M rays) as one graph-captured launch; every item against the oracle."""
+    import torch
+
+    from igx_raytracing_gb300 import HIT_DTYPE
+
+    ntris, nrays = scenes.workload_batch_plan(64)
+    items, host, scenes_ = [], [], []
+    for i, (nt, nr) in enumerate(zip(ntris, nrays)):
+        tris = scenes.random_triangles(int(nt), scenes.seed_for(4, i))
+        bvh = BVH.build(tris)
+        scene = ctx.create_scene(bvh=bvh)
+        rays = scenes.batch_rays(i, int(nr))
+        d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).cuda()
+        out = torch.zeros((len(rays), 4), dtype=torch.float32, device="cuda")
+        items.append((scene, d_rays, None, out, 0))
+        host.append((tris, rays, bvh))
+        scenes_.append(scene)
+    assert int(nrays.sum()) > 20_000_000
+    batch = ctx.create_batch(items)
+    batch.launch()
+    torch.cuda.synchronize()
+    ctx.sync()
+    for i, ((tris, rays, bvh), (_, _, _, out, _)) in enumerate(zip(host, items)):
+        got = out.cpu().numpy().view(HIT_DTYPE).reshape(-1)
+        _check(tris, rays, None, 0, got, bvh, pyoracle.bvh_build(tris), f"batch item {i}", subset=4096,
+               seed=100 + i)
+    batch.close()
+    for s in scenes_:
+        s.close()
+
+
+def test_serving_sample_full_size_scenes(ctx):
+    """Config 5's 32 resident scenes (10K-2M triangles): 160 requests of its
+    request distribution (1K-1M rays, closest or any hit), replayed at
+    2,000 requests/s through the server; every request against the oracle."""
+    from igx_raytracing_gb300 import Server
+
+    rng = np.random.default_rng(scenes.seed_for(5))
+    ntris = scenes.log_uniform_ints(rng, 10_000, 2_000_000, 32)
+    trees, sc = [], []
+    srv = Server(ctx, streams=2)
+    ids = []
+    for i, nt in enumerate(ntris):
+        tris = scenes.random_triangles(int(nt), scenes.seed_for(5, i))
+        bvh = BVH.build(tris)
+        s = ctx.create_scene(bvh=bvh)
+        sc.append(s)
+        trees.append((tris, bvh))
+        ids.append(srv.add_scene(s))
+    n_req = 160
+    arrivals = np.cumsum(rng.exponential(1 / 2000.0, n_req))
+    scene_of = rng.integers(0, 32, n_req)
+    counts = scenes.log_uniform_ints(rng, 1000, 1_000_000, n_req)
+    modes = rng.integers(0, 2, n_req)
+    reqs = []
+    for k in range(n_req):
+        rays = scenes.batch_rays(2000 + k, int(counts[k]))
+        if modes[k]:
+            rays["tmax"] = rng.uniform(0.02, 0.6, len(rays)).astype(np.float32)
+        reqs.append((ids[scene_of[k]], rays, None, int(modes[k]), None))
+    tickets = srv.replay(reqs, arrivals)
+    outs = [srv.wait(t, timeout=120.0)["out"] for t in tickets]
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == n_req and st["rejected"] == 0
+    otrees = {}
+    for k, ((sid, rays, _, mode, _), got) in enumerate(zip(reqs, outs)):
+        j = int(scene_of[k])
+        tris, bvh = trees[j]
+        if j not in otrees:
+            otrees[j] = pyoracle.bvh_build(tris)
+        _check(tris, rays, None, mode, got, bvh, otrees[j], f"request {k} (scene {j})", subset=256,
+               seed=300 + k)
+    for s in sc:
+        s.close()

@@ -62,6 +62,52 @@ def test_static_entry_matches_regular_entry_on_consecutive_calls(ctx, engine_lib
     _same(got4, expect[:1000])
 
 
+def _scene_cases(ctx):
+    """A triangle scene from the host builder (every layout), a mixed scene
+    (spheres, cubes and planes beside the triangles) and a GPU-built scene
+    (BVH2 and BVH4 only)."""
+    tris = scenes.random_triangles(30000, 561, mu=math.log(0.01))
+    mixed = scenes.workload_mixed(20000, 2000, 2000, 4)
+    return [
+        ("host", ctx.create_scene(tris), (0, 1, 2)),
+        ("mixed", ctx.create_scene_mixed(mixed["tris"], mixed["spheres"], mixed["cubes"], mixed["planes"]),
+         (0, 1, 2)),
+        ("gpu", ctx.create_scene_gpu(tris), (0, 1)),
+    ]
+
+
+@pytest.mark.parametrize("case", ["host", "mixed", "gpu"])
+def test_static_entry_matches_regular_entry_per_scene_kind_and_layout(ctx, engine_lib, case):
+    name, scene, layouts = next(c for c in _scene_cases(ctx) if c[0] == case)
+    rays = scenes.incoherent_rays(60000, 562)
+    prev = np.random.default_rng(563).integers(0, 30000, len(rays)).astype(np.uint32)
+    saved = ctx.launch_params
+    try:
+        for layout in layouts:
+            ctx.set_launch_params(layout=layout)
+            expect = scene.trace_geometry(rays, prev)
+            for _ in range(2):  # two calls in a row share the array
+                st, got = _static(engine_lib, ctx, scene, rays, prev)
+                assert st == 0, engine_lib.igxrt_last_error(ctx.handle)
+                _same(got, expect)
+    finally:
+        ctx.set_launch_params(**saved)
+
+
+def test_static_entry_refuses_a_layout_the_scene_lacks(ctx, engine_lib):
+    tris = scenes.random_triangles(5000, 564)
+    scene = ctx.create_scene_gpu(tris)  # GPU-built trees have no BVH8 layout
+    rays = scenes.incoherent_rays(1000, 565)
+    saved = ctx.launch_params
+    try:
+        ctx.set_launch_params(layout=2)
+        st, _ = _static(engine_lib, ctx, scene, rays)
+        assert st == 8  # IGXRT_ERROR_UNSUPPORTED, nothing launched
+        assert b"layout" in engine_lib.igxrt_last_error(ctx.handle)
+    finally:
+        ctx.set_launch_params(**saved)
+
+
 def test_static_entry_allocates_no_device_memory(ctx, engine_lib):
     import torch
 

@@ -502,8 +502,9 @@ typedef struct igxrt_server_options {
 } igxrt_server_options;
 
 /* A ray-query request.  The arrays are host memory owned by the caller and
- * must stay valid until the request completes; pinned memory makes the
- * copies asynchronous. */
+ * must stay valid until the request completes.  Pinned memory makes the
+ * server's copies asynchronous; a copy to or from pageable memory holds the
+ * scheduler thread until it is done, so batches on other streams wait. */
 typedef struct igxrt_request {
     uint32_t scene_id;        /* from igxrt_server_add_scene */
     uint32_t mode;            /* IGXRT_MODE_CLOSEST or IGXRT_MODE_ANY */

@@ -156,13 +156,27 @@ def test_batches_on_different_streams_overlap_on_the_device(ctx):
     """Twelve 150K-ray requests at once on three streams: every batch kernel
     leaves room on the GPU, and the next stream's kernel starts before the
     last warp of the previous one has left (their own %globaltimer stamps),
-    not only queued together."""
+    not only queued together.  The rays and results are in pinned memory, so
+    the server's copies are asynchronous (a copy to or from pageable memory
+    holds the scheduler thread until it is done)."""
+    import torch
+
+    from igx_raytracing_gb300 import HIT_DTYPE, RAY_DTYPE
+
     sc = _scenes(ctx, n=3, seed=7)
     srv = Server(ctx, streams=3, slice_rays=150000, max_batch_rays=150000)
     ids = [srv.add_scene(s) for s in sc]
-    rays = [scenes.incoherent_rays(150000, 700 + k) for k in range(12)]
-    tickets = [srv.submit(ids[k % 3], r) for k, r in enumerate(rays)]
-    outs = [srv.wait(t, timeout=60.0)["out"] for t in tickets]
+
+    def pinned(a, dtype):
+        p = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory().numpy().view(dtype)
+        p[:] = a
+        return p
+
+    rays = [pinned(scenes.incoherent_rays(150000, 700 + k), RAY_DTYPE) for k in range(12)]
+    outs = [pinned(np.zeros(150000, HIT_DTYPE), HIT_DTYPE) for _ in range(12)]
+    tickets = [srv.submit(ids[k % 3], r, out=o) for k, (r, o) in enumerate(zip(rays, outs))]
+    for t in tickets:
+        srv.wait(t, timeout=60.0)
     times = srv.batch_times()
     srv.close()
     for k, o in enumerate(outs):

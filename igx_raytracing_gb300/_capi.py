@@ -83,7 +83,7 @@ class BvhInfo(C.Structure):
 class LaunchParams(C.Structure):
     _fields_ = [("block_size", C.c_uint32), ("stack_depth", C.c_uint32),
                 ("packet_size", C.c_uint32), ("layout", C.c_uint32), ("ctas_per_sm", C.c_uint32),
-                ("refill_lanes", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("refill_lanes", C.c_uint32), ("phase_break", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class BatchItem(C.Structure):

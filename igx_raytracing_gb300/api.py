@@ -341,7 +341,7 @@ class Context:
         check(lib().igxrt_get_launch_params(self._h, C.byref(p)), self._h)
         return {"block_size": p.block_size, "stack_depth": p.stack_depth,
                 "packet_size": p.packet_size, "layout": p.layout, "ctas_per_sm": p.ctas_per_sm,
-                "refill_lanes": p.refill_lanes}
+                "refill_lanes": p.refill_lanes, "phase_break": p.phase_break}
 
     def set_launch_params(self, **kw) -> None:
         cur = self.launch_params
@@ -590,7 +590,7 @@ class Context:
               self._h, "autotune")
         return ({"block_size": p.block_size, "stack_depth": p.stack_depth,
                  "packet_size": p.packet_size, "layout": p.layout, "ctas_per_sm": p.ctas_per_sm,
-                 "refill_lanes": p.refill_lanes}, ms.value)
+                 "refill_lanes": p.refill_lanes, "phase_break": p.phase_break}, ms.value)
 
 
 class Server:

@@ -1,13 +1,14 @@
 // autotune.cpp — picks the batched kernel's launch parameters by timing them.
 //
 // Search: coordinate descent from the context's current parameters over
-// node layout, packet size, refill threshold, block size and shared stack
-// depth (two rounds; a change is kept only when it is at least 1% faster).
+// node layout, packet size, refill threshold, block size, shared stack depth
+// and the node phase's early end (two rounds; a change is kept only when it
+// is at least 1% faster).
 // Each candidate is timed with CUDA events on a private stream over the
 // caller's items (median of `reps` repetitions after one warm-up), as one
 // batched launch or, with IGXRT_TUNE_PLAIN, as one plain launch per item.
 // Results can be cached in a text file, one line per (GPU name, class key):
-//     <gpu>|<key>\t<block> <stack> <packet> <layout> <ctas> <refill>\t<ms>
+//     <gpu>|<key>\t<block> <stack> <packet> <layout> <ctas> <refill> <phase_break>\t<ms>
 // The default class key buckets the workload by item count, total rays,
 // total triangles (powers of two) and the share of any-hit items.
 #include <cuda_runtime.h>
@@ -61,6 +62,8 @@ bool cache_lookup(const char* path, const std::string& key, igxrt_launch_params&
         std::istringstream in(line.substr(t1 + 1, t2 == std::string::npos ? std::string::npos : t2 - t1 - 1));
         igxrt_launch_params q{};
         if (in >> q.block_size >> q.stack_depth >> q.packet_size >> q.layout >> q.ctas_per_sm >> q.refill_lanes) {
+            if (!(in >> q.phase_break))
+                q.phase_break = 0;  // an entry written before the field existed: the default
             p = q;
             ms = t2 == std::string::npos ? 0.f : std::strtof(line.c_str() + t2 + 1, nullptr);
             found = true;  // the last entry for a key wins
@@ -73,8 +76,8 @@ void cache_store(const char* path, const std::string& key, const igxrt_launch_pa
     FILE* f = fopen(path, "a");
     if (!f)
         return;
-    fprintf(f, "%s\t%u %u %u %u %u %u\t%.4f\n", key.c_str(), p.block_size, p.stack_depth,
-            p.packet_size, p.layout, p.ctas_per_sm, p.refill_lanes, ms);
+    fprintf(f, "%s\t%u %u %u %u %u %u %u\t%.4f\n", key.c_str(), p.block_size, p.stack_depth,
+            p.packet_size, p.layout, p.ctas_per_sm, p.refill_lanes, p.phase_break, ms);
     fclose(f);
 }
 
@@ -264,16 +267,21 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
     const std::vector<uint32_t> refills = {1, 2, 4, 8, 16};
     const std::vector<uint32_t> blocks = {64, 128, 256};
     const std::vector<uint32_t> stacks = {8, 16, 32};
+    const std::vector<uint32_t> breaks = {1, 2, 3, 32};
     for (int round = 0; round < 2; ++round) {
         bool changed = false;
-        for (int dim = 0; dim < 5; ++dim) {
-            const std::vector<uint32_t>& vals =
-                dim == 0 ? layouts : dim == 1 ? packets : dim == 2 ? refills : dim == 3 ? blocks : stacks;
+        for (int dim = 0; dim < 6; ++dim) {
+            const std::vector<uint32_t>& vals = dim == 0   ? layouts
+                                                : dim == 1 ? packets
+                                                : dim == 2 ? refills
+                                                : dim == 3 ? blocks
+                                                : dim == 4 ? stacks
+                                                           : breaks;
             for (uint32_t v : vals) {
                 igxrt_launch_params c = cur;
                 uint32_t* field = dim == 0 ? &c.layout : dim == 1 ? &c.packet_size
                                   : dim == 2 ? &c.refill_lanes : dim == 3 ? &c.block_size
-                                             : &c.stack_depth;
+                                  : dim == 4 ? &c.stack_depth : &c.phase_break;
                 if (*field == v)
                     continue;
                 if (dim == 0 && !((mask >> v) & 1u))

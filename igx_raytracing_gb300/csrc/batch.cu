@@ -33,6 +33,7 @@ struct BatchArgs {
     uint32_t packet;
     uint32_t sh_depth;
     uint32_t refill_lanes;
+    uint32_t phase_break;       // node_phase's early end (igxrt_launch_params.phase_break)
     unsigned long long* times;  // optional: {earliest CTA start, latest warp exit}
 };
 
@@ -177,10 +178,12 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
         }
         if (__ballot_sync(0xffffffffu, alive) == 0)
             break;
-        if (alive && !(link & (kLinkWait | kLinkMerge))) {
+        const bool working = alive && !(link & (kLinkWait | kLinkMerge));
+        const uint32_t wmask = __ballot_sync(0xffffffffu, working);
+        if (working) {
             bool overflow = false;
-            while (next >= 0 && next != kRefDone)
-                next = visit_node<LAYOUT, false, MIXED>(nodes, next, r, best, st, overflow, unused);
+            // node phase as in the plain kernels (traverse.cuh: node_phase)
+            node_phase<LAYOUT, false, MIXED>(nodes, wmask, a.phase_break, next, r, best, st, overflow, unused);
             // a plane occluding the ray at its start decides it in this first
             // round only (the lane may next help another ray in the tail)
             bool occluded = occluded_at_start;
@@ -315,6 +318,7 @@ igxrt_status launch_batch(igxrt_context* ctx, const BatchItemDev* d_table, uint3
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;
+    a.phase_break = p.phase_break;
     a.times = times;
     e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess)

@@ -59,6 +59,12 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
     if (out.refill_lanes > 32)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                     format("refill_lanes %u: at most 32", out.refill_lanes));
+    if (!out.phase_break)
+        out.phase_break = 2;
+    if (out.phase_break > 32)
+        return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
+                    format("phase_break %u: 1..31, or 32 for no early end of the node phase",
+                           out.phase_break));
     if (out.block_size < 32 || out.block_size > 256 || out.block_size % 32)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                     format("block_size %u: use a multiple of 32 up to 256", out.block_size));

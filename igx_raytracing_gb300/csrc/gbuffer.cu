@@ -34,6 +34,7 @@ struct GbufferArgs {
     float4* uv_normal;
     uint32_t* status;
     uint32_t sh_depth;
+    uint32_t phase_break;  // node_phase's early end (igxrt_launch_params.phase_break)
 };
 
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
@@ -145,7 +146,10 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < a.tiles; w += warps) {
         const uint32_t ty = w / a.tiles_x, tx = w - ty * a.tiles_x;
         const uint32_t x = tx * 8u + (lane & 7u), y = ty * 4u + (lane >> 3);
-        if (x >= c.width || y >= c.height)
+        // the tile's pixels inside the image trace together (trace_warp)
+        const bool inside = x < c.width && y < c.height;
+        const uint32_t wmask = __ballot_sync(0xffffffffu, inside);
+        if (!inside)
             continue;
         const float3 dir = camera_dir(c, a.inv_w, a.inv_h, x, y);
         const float dx = dir.x, dy = dir.y, dz = dir.z;
@@ -169,11 +173,8 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
         BestHit best;
         bool overflow = false;
         uint32_t rec = 0;
-        if (MIXED)
-            trace_single_mixed<LAYOUT>(a.nodes, a.prims, a.node_count, a.planes, a.plane_count, a.plane_base, r,
-                                       best, st, overflow, rec);
-        else
-            trace_single<LAYOUT, false>(a.nodes, a.prims, a.node_count, r, best, st, overflow);
+        trace_warp<LAYOUT, MIXED>(a.nodes, a.prims, a.node_count, a.planes, a.plane_count, a.plane_base, wmask,
+                                  a.phase_break, r, best, st, overflow, rec);
         if (overflow)
             atomicOr(a.status, kStatusStackOverflow);
         const size_t px = (size_t)y * c.width + x;
@@ -277,6 +278,7 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     a.uv_normal = d_uv;
     a.status = status_word(ctx);
     a.sh_depth = p.stack_depth;
+    a.phase_break = p.phase_break;
     constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
     auto fn = scene->mixed ? (p.layout == B8 ? gbuffer_kernel<B8, true>
                               : p.layout == B4 ? gbuffer_kernel<B4, true> : gbuffer_kernel<B2, true>)

@@ -39,6 +39,7 @@ struct KernelArgs {
     uint32_t packet;
     uint32_t sh_depth;
     uint32_t refill_lanes;
+    uint32_t phase_break;  // node_phase's early end (igxrt_launch_params.phase_break)
     const float4* planes;  // mixed scenes: planes outside the tree
     uint32_t plane_count;
     uint32_t plane_base;   // object id of the first plane
@@ -77,9 +78,9 @@ constexpr int trace_kernel_regs(int layout, bool any, bool mixed) {
 }
 
 // Persistent traversal.  Every lane owns one ray at a time; a warp alternates
-// a node phase (each lane descends until it reaches a leaf or finishes) and a
-// leaf phase (each lane tests one leaf), so lanes at the same kind of work
-// execute together.  Between phases, once `refill_lanes` lanes are idle the
+// a node phase (each lane descends until it reaches a leaf or finishes, or
+// until few lanes still descend: node_phase) and a leaf phase (each lane at
+// a leaf tests it), so lanes at the same kind of work execute together.  Between phases, once `refill_lanes` lanes are idle the
 // warp hands them new rays: one atomicAdd on the global queue claims a
 // packet of `packet` ray indices for the warp, and idle lanes take the next
 // indices in lane order (ballot + popc).  Until the warp finds the queue
@@ -174,11 +175,12 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
         }
         if (__ballot_sync(0xffffffffu, alive) == 0)
             break;  // only reachable once the queue is drained
-        if (alive && !(STEAL && (link & (kLinkWait | kLinkMerge)))) {
+        const bool working = alive && !(STEAL && (link & (kLinkWait | kLinkMerge)));
+        const uint32_t wmask = __ballot_sync(0xffffffffu, working);
+        if (working) {
             bool overflow = false;
-            // node phase
-            while (next >= 0 && next != kRefDone)
-                next = visit_node<LAYOUT, COUNT, MIXED>(a.nodes, next, r, best, st, overflow, nf);
+            // node phase (traverse.cuh: node_phase, which may end it early)
+            node_phase<LAYOUT, COUNT, MIXED>(a.nodes, wmask, a.phase_break, next, r, best, st, overflow, nf);
             // a plane occluding the ray when it started decides it in this
             // first round; the flag must not outlive the ray (the lane may
             // next help another ray's traversal in the tail)
@@ -297,6 +299,7 @@ igxrt_status prepare_trace(igxrt_context* ctx, const TraceRequest& req, const ig
     a.packet = p.packet_size;
     a.sh_depth = p.stack_depth;
     a.refill_lanes = p.refill_lanes;
+    a.phase_break = p.phase_break;
     a.planes = reinterpret_cast<const float4*>(s->planes);
     a.plane_count = s->plane_count;
     a.plane_base = s->plane_base;

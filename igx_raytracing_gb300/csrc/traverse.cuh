@@ -226,6 +226,37 @@ __device__ __forceinline__ bool process_leaf(const float4* __restrict__ prims, i
     return false;
 }
 
+template <int LAYOUT, bool COUNT, bool MIXED>
+__device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, int32_t node,
+                                              const RayState& r, const BestHit& best,
+                                              TraversalStack& st, bool& overflow, uint32_t& nf);
+
+// The node phase of the persistent kernels, run together by the lanes in
+// `wmask` (the warp's working lanes): each lane descends through interior
+// nodes until it holds a leaf or its traversal is over.  A lane that got
+// there first waits for the others (the leaf phase that follows tests the
+// lanes' leaves together), and most waiting happens behind a few lanes with
+// long descents; so once `phase_break` times the lanes still descending is at
+// most the number of lanes waiting (at a leaf, or done), the phase ends and
+// the descending lanes resume in the warp's next round, after the leaves.
+// The order in which each ray visits its nodes and records is the same for
+// every phase_break; phase_break 32 never ends the phase early.
+template <int LAYOUT, bool COUNT, bool MIXED>
+__device__ __forceinline__ void node_phase(const float4* __restrict__ nodes, uint32_t wmask, uint32_t phase_break,
+                                           int32_t& next, const RayState& r, const BestHit& best,
+                                           TraversalStack& st, bool& overflow, uint32_t& nf) {
+    for (;;) {
+        const bool down = next >= 0 && next != kRefDone;
+        const uint32_t dm = __ballot_sync(wmask, down);
+        if (dm == 0)
+            break;
+        if ((uint32_t)__popc(dm) * phase_break <= (uint32_t)__popc(wmask & ~dm))
+            break;
+        if (down)
+            next = visit_node<LAYOUT, COUNT, MIXED>(nodes, next, r, best, st, overflow, nf);
+    }
+}
+
 // 256-bit read-only load (sm_100+): eight floats from a 32-byte aligned address.
 __device__ __forceinline__ void ldg256(const void* p, float4& lo, float4& hi) {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -694,69 +725,41 @@ __device__ __forceinline__ bool test_planes(const float4* __restrict__ planes, u
     return false;
 }
 
-// Whole traversal of one ray by one thread (no refill), in the same order as
-// the persistent kernels.  ANY: returns true at the first occluder.
-// Otherwise `best` ends as the closest hit.
-template <int LAYOUT, bool ANY>
-__device__ __forceinline__ bool trace_single(const float4* __restrict__ nodes,
-                                             const float4* __restrict__ prims, uint32_t node_count,
-                                             const RayState& r, BestHit& best, TraversalStack& st,
-                                             bool& overflow) {
+// Closest hit of one ray per lane, the lanes of `wmask` tracing their rays
+// together (each lane's whole traversal, no refill), in the persistent
+// kernels' order: the node phase (node_phase, with its early end) and the
+// leaf phase alternate until every lane's traversal is over.  MIXED: planes
+// are tested first, best.prim ends as a priority code (id_of_prio gives the
+// object) and best_rec as the best hit's record index, or kRecPlane | plane
+// index.  Every lane of wmask calls this with the same scene.
+template <int LAYOUT, bool MIXED>
+__device__ __forceinline__ void trace_warp(const float4* __restrict__ nodes, const float4* __restrict__ prims,
+                                           uint32_t node_count, const float4* __restrict__ planes,
+                                           uint32_t plane_count, uint32_t plane_base, uint32_t wmask,
+                                           uint32_t phase_break, const RayState& r, BestHit& best,
+                                           TraversalStack& st, bool& overflow, uint32_t& best_rec) {
     best.t = r.tmax_eff;
     best.u = 0.f;
     best.v = 0.f;
-    best.prim = 0;
-    best.tcull = cull_limit(best.t);
-    if (!node_count)
-        return false;
-    st.sp = 0;
-    uint32_t unused = 0;
-    int32_t next = 0;
-    for (;;) {
-        while (next >= 0 && next != kRefDone)
-            next = visit_node<LAYOUT, false>(nodes, next, r, best, st, overflow, unused);
-        if (next == kRefDone)
-            return false;
-        if (process_leaf<ANY, false>(prims, next, r, best, unused))
-            return true;
-        next = st.pop_live(best.tcull);
-        if (next == kRefDone)
-            return false;
-    }
-}
-
-// Closest hit of one ray in a mixed scene by one thread, in the persistent
-// kernels' order: planes first, then the tree.  best.prim ends as a priority
-// code (id_of_prio gives the object) and best_rec as the best hit's record
-// index, or kRecPlane | plane index.
-template <int LAYOUT>
-__device__ __forceinline__ void trace_single_mixed(const float4* __restrict__ nodes,
-                                                   const float4* __restrict__ prims, uint32_t node_count,
-                                                   const float4* __restrict__ planes, uint32_t plane_count,
-                                                   uint32_t plane_base, const RayState& r, BestHit& best,
-                                                   TraversalStack& st, bool& overflow, uint32_t& best_rec) {
-    best.t = r.tmax_eff;
-    best.u = 0.f;
-    best.v = 0.f;
-    best.prim = kPrioNone;
+    best.prim = MIXED ? kPrioNone : 0u;
     best.tcull = cull_limit(best.t);
     best_rec = 0xffffffffu;
-    if (plane_count)
+    if (MIXED && plane_count)
         test_planes<false>(planes, plane_count, plane_base, r, best, &best_rec);
     if (!node_count)
         return;
     st.sp = 0;
     uint32_t unused = 0;
     int32_t next = 0;
-    for (;;) {
-        while (next >= 0 && next != kRefDone)
-            next = visit_node<LAYOUT, false, true>(nodes, next, r, best, st, overflow, unused);
-        if (next == kRefDone)
-            return;
-        process_leaf_mixed<false>(prims, next, r, best, nullptr, &best_rec);
-        next = st.pop_live(best.tcull);
-        if (next == kRefDone)
-            return;
+    while (__ballot_sync(wmask, next != kRefDone)) {
+        node_phase<LAYOUT, false, MIXED>(nodes, wmask, phase_break, next, r, best, st, overflow, unused);
+        if (next < 0) {
+            if (MIXED)
+                process_leaf_mixed<false>(prims, next, r, best, nullptr, &best_rec);
+            else
+                process_leaf<false, false>(prims, next, r, best, unused);
+            next = st.pop_live(best.tcull);
+        }
     }
 }
 

@@ -369,7 +369,15 @@ typedef struct igxrt_launch_params {
     uint32_t ctas_per_sm; /* persistent CTAs per SM, 0 = as many as fit */
     uint32_t refill_lanes;/* a warp refetches rays once this many of its lanes
                              are idle (1..32); 0 = 8 */
-    uint32_t reserved[2];
+    uint32_t phase_break; /* a warp's lanes descend through interior nodes
+                             together, then test their leaves together; the
+                             descent ends early once phase_break times the
+                             lanes still descending is at most the number of
+                             lanes waiting (at a leaf, or done), and those
+                             lanes resume after the leaves.  1..31; 32 = no
+                             early end (every lane reaches a leaf first);
+                             0 = 2.  Results do not depend on it. */
+    uint32_t reserved;
 } igxrt_launch_params;
 
 igxrt_status igxrt_set_launch_params(igxrt_context* ctx, const igxrt_launch_params* p);
@@ -461,7 +469,7 @@ igxrt_status igxrt_trace_batch(igxrt_context* ctx, const igxrt_batch_item* items
                                void* stream);
 
 /* Autotuner: times candidate launch parameters (node layout, block size,
- * shared stack depth, packet size, refill threshold) on the given items and
+ * shared stack depth, packet size, refill threshold, phase break) on the given items and
  * returns the fastest.  With a cache file, results are stored under
  * (GPU name, class key) and reused without timing.  By default a candidate
  * is timed as one batched launch over the items (igxrt_trace_batch); with

@@ -42,6 +42,7 @@ def _case(seed):
                   stack_depth=int(rng.choice([0, 1, 2, 4, 8, 16])),
                   packet_size=int(rng.choice([32, 64, 96, 256])),
                   refill_lanes=int(rng.choice([1, 4, 8, 16, 32])),
+                  phase_break=int(rng.choice([1, 2, 3, 7, 32])),
                   layout=int(rng.integers(0, 3)))
     return tris, rays, prev, params
 

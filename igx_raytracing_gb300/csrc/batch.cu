@@ -180,10 +180,11 @@ __global__ void __launch_bounds__(256) batch_kernel(BatchArgs a) {
             break;
         const bool working = alive && !(link & (kLinkWait | kLinkMerge));
         const uint32_t wmask = __ballot_sync(0xffffffffu, working);
+        // node phase as in the plain kernels, every lane taking part
+        // (traverse.cuh: node_phase)
+        bool overflow = false;
+        node_phase<LAYOUT, false, MIXED>(nodes, working, wmask, a.phase_break, next, r, best, st, overflow, unused);
         if (working) {
-            bool overflow = false;
-            // node phase as in the plain kernels (traverse.cuh: node_phase)
-            node_phase<LAYOUT, false, MIXED>(nodes, wmask, a.phase_break, next, r, best, st, overflow, unused);
             // a plane occluding the ray at its start decides it in this first
             // round only (the lane may next help another ray in the tail)
             bool occluded = occluded_at_start;

@@ -146,12 +146,11 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < a.tiles; w += warps) {
         const uint32_t ty = w / a.tiles_x, tx = w - ty * a.tiles_x;
         const uint32_t x = tx * 8u + (lane & 7u), y = ty * 4u + (lane >> 3);
-        // the tile's pixels inside the image trace together (trace_warp)
+        // the tile's pixels inside the image trace together (trace_warp);
+        // the lanes outside it take part in the warp's ballots only
         const bool inside = x < c.width && y < c.height;
         const uint32_t wmask = __ballot_sync(0xffffffffu, inside);
-        if (!inside)
-            continue;
-        const float3 dir = camera_dir(c, a.inv_w, a.inv_h, x, y);
+        const float3 dir = camera_dir(c, a.inv_w, a.inv_h, inside ? x : 0u, inside ? y : 0u);
         const float dx = dir.x, dy = dir.y, dz = dir.z;
         RayState r;
         r.ox = c.eye[0];
@@ -173,10 +172,12 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
         BestHit best;
         bool overflow = false;
         uint32_t rec = 0;
-        trace_warp<LAYOUT, MIXED>(a.nodes, a.prims, a.node_count, a.planes, a.plane_count, a.plane_base, wmask,
-                                  a.phase_break, r, best, st, overflow, rec);
+        trace_warp<LAYOUT, MIXED>(a.nodes, a.prims, a.node_count, a.planes, a.plane_count, a.plane_base, inside,
+                                  wmask, a.phase_break, r, best, st, overflow, rec);
         if (overflow)
             atomicOr(a.status, kStatusStackOverflow);
+        if (!inside)
+            continue;
         const size_t px = (size_t)y * c.width + x;
         // raygen.comp:39-44: a miss is hitT == noHit
         if (best.t < IGXRT_NO_HIT) {

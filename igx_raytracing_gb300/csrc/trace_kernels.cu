@@ -177,10 +177,11 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
             break;  // only reachable once the queue is drained
         const bool working = alive && !(STEAL && (link & (kLinkWait | kLinkMerge)));
         const uint32_t wmask = __ballot_sync(0xffffffffu, working);
+        // node phase: every lane of the warp takes part, the working lanes
+        // descend (traverse.cuh: node_phase, which may end it early)
+        bool overflow = false;
+        node_phase<LAYOUT, COUNT, MIXED>(a.nodes, working, wmask, a.phase_break, next, r, best, st, overflow, nf);
         if (working) {
-            bool overflow = false;
-            // node phase (traverse.cuh: node_phase, which may end it early)
-            node_phase<LAYOUT, COUNT, MIXED>(a.nodes, wmask, a.phase_break, next, r, best, st, overflow, nf);
             // a plane occluding the ray when it started decides it in this
             // first round; the flag must not outlive the ray (the lane may
             // next help another ray's traversal in the tail)

@@ -231,23 +231,26 @@ __device__ __forceinline__ int32_t visit_node(const float4* __restrict__ nodes, 
                                               const RayState& r, const BestHit& best,
                                               TraversalStack& st, bool& overflow, uint32_t& nf);
 
-// The node phase of the persistent kernels, run together by the lanes in
-// `wmask` (the warp's working lanes): each lane descends through interior
-// nodes until it holds a leaf or its traversal is over.  A lane that got
-// there first waits for the others (the leaf phase that follows tests the
-// lanes' leaves together), and most waiting happens behind a few lanes with
-// long descents; so once `phase_break` times the lanes still descending is at
-// most the number of lanes waiting (at a leaf, or done), the phase ends and
-// the descending lanes resume in the warp's next round, after the leaves.
-// The order in which each ray visits its nodes and records is the same for
-// every phase_break; phase_break 32 never ends the phase early.
+// The node phase of the persistent kernels, called by all 32 lanes of the
+// warp together (every ballot names the whole warp); the lanes with
+// `working` set (their set is `wmask`) each descend through interior nodes
+// until they hold a leaf or their traversal is over, the others only take
+// part in the ballots.  A working lane that got there first waits for the
+// others (the leaf phase that follows tests the lanes' leaves together), and
+// most waiting happens behind a few lanes with long descents; so once
+// `phase_break` times the lanes still descending is at most the number of
+// working lanes waiting (at a leaf, or done), the phase ends and the
+// descending lanes resume in the warp's next round, after the leaves.  The
+// order in which each ray visits its nodes and records is the same for every
+// phase_break; phase_break 32 never ends the phase early.
 template <int LAYOUT, bool COUNT, bool MIXED>
-__device__ __forceinline__ void node_phase(const float4* __restrict__ nodes, uint32_t wmask, uint32_t phase_break,
-                                           int32_t& next, const RayState& r, const BestHit& best,
-                                           TraversalStack& st, bool& overflow, uint32_t& nf) {
+__device__ __forceinline__ void node_phase(const float4* __restrict__ nodes, bool working, uint32_t wmask,
+                                           uint32_t phase_break, int32_t& next, const RayState& r,
+                                           const BestHit& best, TraversalStack& st, bool& overflow,
+                                           uint32_t& nf) {
     for (;;) {
-        const bool down = next >= 0 && next != kRefDone;
-        const uint32_t dm = __ballot_sync(wmask, down);
+        const bool down = working && next >= 0 && next != kRefDone;
+        const uint32_t dm = __ballot_sync(0xffffffffu, down);
         if (dm == 0)
             break;
         if ((uint32_t)__popc(dm) * phase_break <= (uint32_t)__popc(wmask & ~dm))
@@ -725,34 +728,36 @@ __device__ __forceinline__ bool test_planes(const float4* __restrict__ planes, u
     return false;
 }
 
-// Closest hit of one ray per lane, the lanes of `wmask` tracing their rays
-// together (each lane's whole traversal, no refill), in the persistent
-// kernels' order: the node phase (node_phase, with its early end) and the
-// leaf phase alternate until every lane's traversal is over.  MIXED: planes
-// are tested first, best.prim ends as a priority code (id_of_prio gives the
-// object) and best_rec as the best hit's record index, or kRecPlane | plane
-// index.  Every lane of wmask calls this with the same scene.
+// Closest hit of one ray per lane, called by all 32 lanes of the warp
+// together with the same scene; the lanes with `active` set (their set is
+// `wmask`) trace their rays (each lane's whole traversal, no refill) in the
+// persistent kernels' order: the node phase (node_phase, with its early end)
+// and the leaf phase alternate until every lane's traversal is over.  MIXED:
+// planes are tested first, best.prim ends as a priority code (id_of_prio
+// gives the object) and best_rec as the best hit's record index, or
+// kRecPlane | plane index.
 template <int LAYOUT, bool MIXED>
 __device__ __forceinline__ void trace_warp(const float4* __restrict__ nodes, const float4* __restrict__ prims,
                                            uint32_t node_count, const float4* __restrict__ planes,
-                                           uint32_t plane_count, uint32_t plane_base, uint32_t wmask,
-                                           uint32_t phase_break, const RayState& r, BestHit& best,
-                                           TraversalStack& st, bool& overflow, uint32_t& best_rec) {
+                                           uint32_t plane_count, uint32_t plane_base, bool active,
+                                           uint32_t wmask, uint32_t phase_break, const RayState& r,
+                                           BestHit& best, TraversalStack& st, bool& overflow,
+                                           uint32_t& best_rec) {
     best.t = r.tmax_eff;
     best.u = 0.f;
     best.v = 0.f;
     best.prim = MIXED ? kPrioNone : 0u;
     best.tcull = cull_limit(best.t);
     best_rec = 0xffffffffu;
-    if (MIXED && plane_count)
+    if (MIXED && plane_count && active)
         test_planes<false>(planes, plane_count, plane_base, r, best, &best_rec);
     if (!node_count)
         return;
     st.sp = 0;
     uint32_t unused = 0;
-    int32_t next = 0;
-    while (__ballot_sync(wmask, next != kRefDone)) {
-        node_phase<LAYOUT, false, MIXED>(nodes, wmask, phase_break, next, r, best, st, overflow, unused);
+    int32_t next = active ? 0 : kRefDone;
+    while (__ballot_sync(0xffffffffu, next != kRefDone)) {
+        node_phase<LAYOUT, false, MIXED>(nodes, active, wmask, phase_break, next, r, best, st, overflow, unused);
         if (next < 0) {
             if (MIXED)
                 process_leaf_mixed<false>(prims, next, r, best, nullptr, &best_rec);

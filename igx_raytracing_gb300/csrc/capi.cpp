@@ -219,7 +219,7 @@ igxrt_status igxrt::read_status(igxrt_context* ctx) {
     if (word) {
         cudaMemset(status_word(ctx), 0, sizeof(uint32_t));
         return fail(ctx, IGXRT_ERROR_KERNEL_STATUS,
-                    format("kernel error word 0x%x (1 = traversal stack overflow)", word));
+                    format("kernel error word 0x%x (1 = traversal stack overflow, 2 = round limit)", word));
     }
     return IGXRT_OK;
 }

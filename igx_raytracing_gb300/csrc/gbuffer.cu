@@ -149,7 +149,6 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
         // the tile's pixels inside the image trace together (trace_warp);
         // the lanes outside it take part in the warp's ballots only
         const bool inside = x < c.width && y < c.height;
-        const uint32_t wmask = __ballot_sync(0xffffffffu, inside);
         const float3 dir = camera_dir(c, a.inv_w, a.inv_h, inside ? x : 0u, inside ? y : 0u);
         const float dx = dir.x, dy = dir.y, dz = dir.z;
         RayState r;
@@ -172,10 +171,13 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
         BestHit best;
         bool overflow = false;
         uint32_t rec = 0;
-        trace_warp<LAYOUT, MIXED>(a.nodes, a.prims, a.node_count, a.planes, a.plane_count, a.plane_base, inside,
-                                  wmask, a.phase_break, r, best, st, overflow, rec);
+        const uint32_t gave_up = trace_warp<LAYOUT, MIXED>(a.nodes, a.prims, a.node_count, a.planes,
+                                                           a.plane_count, a.plane_base, inside, a.phase_break, r,
+                                                           best, st, overflow, rec);
         if (overflow)
             atomicOr(a.status, kStatusStackOverflow);
+        if (gave_up && lane == 0)
+            atomicOr(a.status, gave_up);
         if (!inside)
             continue;
         const size_t px = (size_t)y * c.width + x;

@@ -130,6 +130,6 @@ extern "C" igxrt_status igxrt_trace_closest_static(igxrt_context* ctx, const igx
         return cuda_fail(ctx, e, "static scratch trace");
     if (status_word)
         return fail(ctx, IGXRT_ERROR_KERNEL_STATUS,
-                    format("kernel error word 0x%x (1 = traversal stack overflow)", status_word));
+                    format("kernel error word 0x%x (1 = traversal stack overflow, 2 = round limit)", status_word));
     return IGXRT_OK;
 }

@@ -728,21 +728,29 @@ __device__ __forceinline__ bool test_planes(const float4* __restrict__ planes, u
     return false;
 }
 
+// Rounds of trace_warp after which a warp gives up and reports
+// kStatusRoundLimit (each round advances at least one lane by a node or a
+// leaf, so a correct traversal stays far below this).
+constexpr uint32_t kStatusRoundLimit = 2u;
+constexpr uint32_t kTraceWarpRounds = 1u << 22;
+
 // Closest hit of one ray per lane, called by all 32 lanes of the warp
-// together with the same scene; the lanes with `active` set (their set is
-// `wmask`) trace their rays (each lane's whole traversal, no refill) in the
-// persistent kernels' order: the node phase (node_phase, with its early end)
-// and the leaf phase alternate until every lane's traversal is over.  MIXED:
-// planes are tested first, best.prim ends as a priority code (id_of_prio
-// gives the object) and best_rec as the best hit's record index, or
-// kRecPlane | plane index.
+// together with the same scene; the lanes with `active` set trace their rays
+// (each lane's whole traversal, no refill) in the persistent kernels' order:
+// the node phase (node_phase, with its early end) and the leaf phase
+// alternate until every lane's traversal is over.  Each round's working
+// lanes are those still tracing, so a finished lane never counts as waiting
+// (the early end would otherwise keep ending the phase before the lanes
+// still descending move).  MIXED: planes are tested first, best.prim ends as
+// a priority code (id_of_prio gives the object) and best_rec as the best
+// hit's record index, or kRecPlane | plane index.  Returns kStatusRoundLimit
+// if the warp gave up, else 0.
 template <int LAYOUT, bool MIXED>
-__device__ __forceinline__ void trace_warp(const float4* __restrict__ nodes, const float4* __restrict__ prims,
-                                           uint32_t node_count, const float4* __restrict__ planes,
-                                           uint32_t plane_count, uint32_t plane_base, bool active,
-                                           uint32_t wmask, uint32_t phase_break, const RayState& r,
-                                           BestHit& best, TraversalStack& st, bool& overflow,
-                                           uint32_t& best_rec) {
+__device__ __forceinline__ uint32_t trace_warp(const float4* __restrict__ nodes, const float4* __restrict__ prims,
+                                               uint32_t node_count, const float4* __restrict__ planes,
+                                               uint32_t plane_count, uint32_t plane_base, bool active,
+                                               uint32_t phase_break, const RayState& r, BestHit& best,
+                                               TraversalStack& st, bool& overflow, uint32_t& best_rec) {
     best.t = r.tmax_eff;
     best.u = 0.f;
     best.v = 0.f;
@@ -752,12 +760,18 @@ __device__ __forceinline__ void trace_warp(const float4* __restrict__ nodes, con
     if (MIXED && plane_count && active)
         test_planes<false>(planes, plane_count, plane_base, r, best, &best_rec);
     if (!node_count)
-        return;
+        return 0u;
     st.sp = 0;
     uint32_t unused = 0;
     int32_t next = active ? 0 : kRefDone;
-    while (__ballot_sync(0xffffffffu, next != kRefDone)) {
-        node_phase<LAYOUT, false, MIXED>(nodes, active, wmask, phase_break, next, r, best, st, overflow, unused);
+    for (uint32_t round = 0;; ++round) {
+        const bool tracing = next != kRefDone;
+        const uint32_t live = __ballot_sync(0xffffffffu, tracing);
+        if (live == 0)
+            return 0u;
+        if (round == kTraceWarpRounds)
+            return kStatusRoundLimit;
+        node_phase<LAYOUT, false, MIXED>(nodes, tracing, live, phase_break, next, r, best, st, overflow, unused);
         if (next < 0) {
             if (MIXED)
                 process_leaf_mixed<false>(prims, next, r, best, nullptr, &best_rec);

@@ -263,7 +263,7 @@ extern "C" igxrt_status igxrt_autotune(igxrt_context* ctx, const igxrt_batch_ite
         return fail(ctx, IGXRT_ERROR_CUDA, "autotune: the starting parameters do not launch");
 
     const std::vector<uint32_t> layouts = {IGXRT_LAYOUT_BVH2, IGXRT_LAYOUT_BVH4, IGXRT_LAYOUT_BVH8};
-    const std::vector<uint32_t> packets = {32, 64, 128, 256};
+    const std::vector<uint32_t> packets = {8, 16, 32, 64, 128, 256};
     const std::vector<uint32_t> refills = {1, 2, 4, 8, 16};
     const std::vector<uint32_t> blocks = {64, 128, 256};
     const std::vector<uint32_t> stacks = {8, 16, 32};

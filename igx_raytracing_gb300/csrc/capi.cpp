@@ -51,7 +51,7 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
     if (!out.block_size)
         out.block_size = 128;
     if (!out.packet_size)
-        out.packet_size = 32;
+        out.packet_size = 16;
     if (out.stack_depth == 0 && in.block_size == 0 && in.packet_size == 0)
         out.stack_depth = 16;
     if (!out.refill_lanes)
@@ -68,9 +68,9 @@ igxrt_status resolve_params(igxrt_context* ctx, const igxrt_launch_params& in, i
     if (out.block_size < 32 || out.block_size > 256 || out.block_size % 32)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                     format("block_size %u: use a multiple of 32 up to 256", out.block_size));
-    if (out.packet_size < 32 || out.packet_size > 4096 || out.packet_size % 32)
+    if (out.packet_size < 8 || out.packet_size > 4096 || out.packet_size % 8)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
-                    format("packet_size %u: use a multiple of 32 up to 4096", out.packet_size));
+                    format("packet_size %u: use a multiple of 8 up to 4096", out.packet_size));
     if (out.stack_depth > 64)
         return fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT,
                     format("stack_depth %u: at most 64 shared entries", out.stack_depth));

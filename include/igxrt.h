@@ -364,7 +364,7 @@ typedef struct igxrt_launch_params {
     uint32_t stack_depth; /* shared-memory stack entries per thread (at most 64);
                              deeper entries spill to local memory; 0 = 16 */
     uint32_t packet_size; /* rays a warp claims per queue fetch: a multiple of
-                             32 up to 4096; 0 = 32 */
+                             8 up to 4096; 0 = 16 */
     uint32_t layout;      /* IGXRT_LAYOUT_* */
     uint32_t ctas_per_sm; /* persistent CTAs per SM, 0 = as many as fit */
     uint32_t refill_lanes;/* a warp refetches rays once this many of its lanes

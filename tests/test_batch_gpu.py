@@ -65,7 +65,7 @@ def params(ctx):
 
 
 @pytest.mark.parametrize("layout", [0, 1, 2])
-@pytest.mark.parametrize("packet,refill", [(32, 1), (64, 8), (256, 32)])
+@pytest.mark.parametrize("packet,refill", [(8, 8), (16, 4), (32, 1), (64, 8), (256, 32)])
 def test_trace_batch_matches_plain(params, layout, packet, refill):
     ctx = params
     ctx.set_launch_params(layout=layout, packet_size=packet, refill_lanes=refill)
@@ -118,7 +118,7 @@ def test_autotune_and_cache(ctx, tmp_path):
     items, plain = _items(ctx, seed=9, nscenes=6, with_empty=False)
     cache = os.path.join(tmp_path, "tune.txt")
     p, ms = ctx.autotune(items, reps=2, cache_path=cache, class_key="unit-test")
-    assert ms > 0 and p["layout"] in (0, 1, 2) and p["packet_size"] in (32, 64, 128, 256)
+    assert ms > 0 and p["layout"] in (0, 1, 2) and p["packet_size"] in (8, 16, 32, 64, 128, 256)
     text = open(cache).read()
     assert "unit-test" in text
     p2, ms2 = ctx.autotune(items, reps=2, cache_path=cache, class_key="unit-test")

@@ -40,7 +40,7 @@ def _case(seed):
     prev = np.where(rng.random(n_rays) < 0.3, rng.integers(0, len(tris), n_rays), 0xFFFFFFFF).astype(np.uint32)
     params = dict(block_size=int(rng.choice([32, 64, 128, 256])),
                   stack_depth=int(rng.choice([0, 1, 2, 4, 8, 16])),
-                  packet_size=int(rng.choice([32, 64, 96, 256])),
+                  packet_size=int(rng.choice([8, 16, 24, 32, 64, 96, 256])),
                   refill_lanes=int(rng.choice([1, 4, 8, 16, 32])),
                   phase_break=int(rng.choice([1, 2, 3, 7, 32])),
                   layout=int(rng.integers(0, 3)))

@@ -72,7 +72,7 @@ def test_small_workload_all_rays_vs_brute_force(ctx):
 
 @pytest.mark.parametrize("block,depth,packet", [(32, 0, 32), (64, 8, 64), (128, 16, 64),
                                                 (256, 32, 128), (128, 64, 4096), (256, 0, 32),
-                                                (128, 2, 32)])
+                                                (128, 2, 32), (128, 16, 8), (64, 16, 24)])
 @pytest.mark.parametrize("layout", LAYOUTS)
 def test_launch_shapes_agree(params, block, depth, packet, layout):
     ctx = params
@@ -162,6 +162,8 @@ def test_host_pointer_without_flag_is_rejected(ctx, engine_lib):
     assert b"IGXRT_TRACE_HOST_MEMORY" in engine_lib.igxrt_last_error(ctx.handle)
     with pytest.raises(IgxrtError):
         ctx.set_launch_params(block_size=48)
+    with pytest.raises(IgxrtError):
+        ctx.set_launch_params(packet_size=12)  # not a multiple of 8
 
 
 def test_determinism_and_permutation_invariance(ctx):

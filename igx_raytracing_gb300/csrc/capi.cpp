@@ -518,6 +518,7 @@ igxrt_status igxrt_scene_destroy(igxrt_scene* scene) {
         cudaDeviceSynchronize();
         cudaFree(scene->d_mem);
         cudaFree(scene->refit_boxes);
+        cudaFree(scene->refit_unions);
     }
     delete scene;
     return IGXRT_OK;

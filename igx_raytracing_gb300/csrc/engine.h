@@ -62,6 +62,10 @@ struct igxrt_scene {
     // 0}), written by the record pass and read by the node climb; allocated
     // at the scene's first GPU refit, freed with the scene
     float4* refit_boxes = nullptr;
+    // GPU refit scratch, two float4 per node of BVH2, then of BVH4: the union
+    // of the node's slot boxes ({lo, 0}, {hi, 0}), written by the climb for
+    // the parent's thread; allocated and freed with refit_boxes
+    float4* refit_unions = nullptr;
 
     // A layout can be traced when the tree has it; an empty scene has none
     // and traces as all misses in every layout.

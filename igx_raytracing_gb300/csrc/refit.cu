@@ -12,13 +12,15 @@
 //      corners) and the scene's triangle and plane copies are rewritten, and
 //      every record's object box is stored in leaf order beside its leaf_end
 //      flag (the scene's refit scratch);
-//   3. nodes: a thread per node whose children are all leaves writes that
-//      node's slot boxes (a leaf slot from the stored boxes: one contiguous
-//      read per record, shared by the BVH2 and BVH4 climbs), then climbs
-//      through the parent links.  At each parent
-//      an atomic arrival counter lets only the thread of the last interior child
-//      go on, so every node is written once, after all of its children.  Nothing
-//      waits on another thread: a thread either continues or exits;
+//   3. nodes: a thread per node writes the node's leaf slots (from the stored
+//      boxes: one contiguous read per record, shared by the BVH2 and BVH4
+//      trees) and arrives at the node; each interior child's climber arrives
+//      there too.  The last of the node's arrivals (an atomic counter per
+//      node) writes its interior slots from the children's union boxes, stores
+//      the node's own union box for its parent and climbs on; the others exit.
+//      A climber so waits on two round trips per level (the arrival, then the
+//      node's slots and its children's unions), and nothing waits on another
+//      thread: a thread either continues or exits;
 //   4. BVH8: every compressed node re-quantized from the BVH2 boxes its slots
 //      were built from (eight lanes per node).
 // Boxes follow the host builder exactly (same min/max argument order, padded by
@@ -126,7 +128,8 @@ struct RefitArgs {
     igxrt_bvh8_node* nodes8;
     const uint32_t* src8;
     uint32_t n8;
-    float4* boxes;  // per record, in leaf order: {lo, leaf_end}, {hi, 0}
+    float4* boxes;   // per record, in leaf order: {lo, leaf_end}, {hi, 0}
+    float4* unions;  // per node of BVH2, then of BVH4: {lo, 0}, {hi, 0}
 };
 
 static_assert(kRefitStateWords == 8, "refit state words");
@@ -205,54 +208,63 @@ __device__ Box leaf_box(const RefitArgs& a, int32_t ref, float pad) {
     return b;
 }
 
-// Writes every non-empty slot of `node`: a leaf slot from its objects, an
-// interior slot as the union of the child node's (already written) slots.
+// Pass 3 for one tree.  The thread of `node` writes the node's leaf slots,
+// then every thread arrives at its node: a node takes one arrival from its
+// own thread and one from the climber of each interior child, and the last
+// one (the counter's acquire-release add makes every earlier arrival's
+// writes visible to it) finishes the node: its interior slots from the
+// children's stored unions, the node's own union (slots folded in slot
+// order, as the host refit folds a child node's slots) stored for the
+// parent, and on to the parent.  The slots and refs it reads are loaded
+// after its arrival; the refs alone, which a refit never changes, are read
+// before it.
 template <int LAYOUT>
-__device__ void refit_node(const RefitArgs& a, typename NodeOps<LAYOUT>::Node* nodes, uint32_t node,
-                           float pad) {
+__device__ void refit_climb(const RefitArgs& a, uint32_t node, float pad) {
     using Ops = NodeOps<LAYOUT>;
+    using Node = typename Ops::Node;
+    Node* nodes = static_cast<Node*>(LAYOUT == IGXRT_LAYOUT_BVH2 ? a.nodes2 : a.nodes4);
+    const uint32_t* parents = LAYOUT == IGXRT_LAYOUT_BVH2 ? a.parents2 : a.parents4;
+    const uint32_t base = LAYOUT == IGXRT_LAYOUT_BVH2 ? 0u : a.n2;
+    uint32_t* arrive = a.state + kRefitStateWords + base;
+    float4* unions = a.unions + 2 * (size_t)base;
     float f[Ops::kFloats];
     Ops::load(nodes + node, f);
     for (int c = 0; c < Ops::kSlots; ++c) {
-        if (Ops::empty(f, c))
+        if (Ops::empty(f, c) || Ops::child(f, c) >= 0)
             continue;
-        const int32_t ref = Ops::child(f, c);
-        Box b;
-        if (ref < 0) {
-            b = leaf_box(a, ref, pad);
-        } else {
-            float g[Ops::kFloats];
-            Ops::load(nodes + ref, g);
-            b.reset();
-            for (int s = 0; s < Ops::kSlots; ++s) {
-                if (Ops::empty(g, s))
-                    continue;
-                Box gb;
-                Ops::get(g, s, gb);
-                b.grow(gb);
-            }
-        }
-        Ops::put(nodes + node, c, b);
+        Ops::put(nodes + node, c, leaf_box(a, Ops::child(f, c), pad));
     }
-}
-
-template <int LAYOUT>
-__device__ void refit_climb(const RefitArgs& a, uint32_t node, float pad) {
-    using Node = typename NodeOps<LAYOUT>::Node;
-    Node* nodes = static_cast<Node*>(LAYOUT == IGXRT_LAYOUT_BVH2 ? a.nodes2 : a.nodes4);
-    const uint32_t* parents = LAYOUT == IGXRT_LAYOUT_BVH2 ? a.parents2 : a.parents4;
-    uint32_t* arrive = a.state + kRefitStateWords + (LAYOUT == IGXRT_LAYOUT_BVH2 ? 0 : a.n2);
-    if (interior_children<LAYOUT>(nodes + node) != 0)
-        return;  // some child's thread reaches this node
     for (;;) {
-        refit_node<LAYOUT>(a, nodes, node, pad);
+        int need = 1;
+        for (int c = 0; c < Ops::kSlots; ++c)
+            need += (!Ops::empty(f, c) && Ops::child(f, c) >= 0) ? 1 : 0;
         const uint32_t p = parents[node];
+        if (arrive_at(arrive + node) + 1u != (uint32_t)need)
+            return;  // another arrival at this node is still to come
+        Ops::load(nodes + node, f);
+        Box u;
+        u.reset();
+        for (int c = 0; c < Ops::kSlots; ++c) {
+            if (Ops::empty(f, c))
+                continue;
+            const int32_t ref = Ops::child(f, c);
+            Box b;
+            if (ref >= 0) {
+                const float4 l = __ldcg(unions + 2 * (size_t)ref), h = __ldcg(unions + 2 * (size_t)ref + 1);
+                b.lo[0] = l.x, b.lo[1] = l.y, b.lo[2] = l.z;
+                b.hi[0] = h.x, b.hi[1] = h.y, b.hi[2] = h.z;
+                Ops::put(nodes + node, c, b);
+            } else {
+                Ops::get(f, c, b);
+            }
+            u.grow(b);
+        }
         if (p == kNoParent)
             return;
-        const uint32_t need = (uint32_t)interior_children<LAYOUT>(nodes + p);
-        if (arrive_at(arrive + p) + 1u != need)
-            return;  // a sibling's thread is still below; it will come up
+        __stcg(unions + 2 * (size_t)node, make_float4(u.lo[0], u.lo[1], u.lo[2], 0.f));
+        __stcg(unions + 2 * (size_t)node + 1, make_float4(u.hi[0], u.hi[1], u.hi[2], 0.f));
         node = p;
+        Ops::load(nodes + node, f);  // refs only: its slots are read again after the arrival
     }
 }
 
@@ -408,6 +420,14 @@ igxrt_status igxrt_scene_refit(igxrt_context* ctx, igxrt_scene* scene, const igx
         }
     }
     a.boxes = scene->refit_boxes;
+    if (a.n2 + a.n4 && !scene->refit_unions) {
+        const cudaError_t e = cudaMalloc(&scene->refit_unions, 2 * sizeof(float4) * ((size_t)a.n2 + a.n4));
+        if (e != cudaSuccess) {
+            scene->refit_unions = nullptr;
+            return cuda_fail(ctx, e, "refit scratch allocation");
+        }
+    }
+    a.unions = scene->refit_unions;
     const size_t words = kRefitStateWords + (size_t)a.n2 + a.n4;
     cudaError_t e = cudaMemsetAsync(a.state, 0, words * sizeof(uint32_t), s);
     if (e != cudaSuccess)

@@ -997,6 +997,19 @@ def measure_serve(args, ctx, device: int, world: int, duration: float) -> dict:
         srv.close()
         return st, lat, clk, times
 
+    def timeline(lat, window_s=1.0):
+        # per window of arrival time: how many requests, their p50, p99 and
+        # max latency; a stall of the host shows as a window where every size
+        # class is late at once
+        out = []
+        edges = np.arange(0.0, float(arrivals[-1]) + window_s, window_s)
+        for lo in edges[:-1]:
+            m = (arrivals >= lo) & (arrivals < lo + window_s)
+            if m.any():
+                out.append([round(float(lo), 1), int(m.sum()), round(float(np.percentile(lat[m], 50)), 3),
+                            round(float(np.percentile(lat[m], 99)), 3), round(float(lat[m].max()), 3)])
+        return out
+
     def classes(lat):
         out = {}
         for name, lo, hi in (("lt10k", 0, 10_000), ("10k_100k", 10_000, 100_000), ("ge100k", 100_000, 1 << 40)):
@@ -1031,7 +1044,9 @@ def measure_serve(args, ctx, device: int, world: int, duration: float) -> dict:
                         "mean_ms": round(st["mean_ms"], 3), "max_ms": round(st["max_ms"], 3),
                         "batches": st["batches"], "peak_memory_gib": round(st["peak_memory_bytes"] / 2**30, 3),
                         "peak_pending": st["peak_pending"], "rejected": st["rejected"],
-                        "by_size": classes(srv_lat)},
+                        "by_size": classes(srv_lat),
+                        "timeline": {"columns": ["from_s", "requests", "p50_ms", "p99_ms", "max_ms"],
+                                     "windows": timeline(srv_lat)}},
             "device_overlap": _device_overlap(times),
             "plain_server": {"p50_ms": round(pst["p50_ms"], 3), "p99_ms": round(pst["p99_ms"], 3),
                              "mrays_s": round(pst["rays_completed"] / plain_span / 1e6, 3),

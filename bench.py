@@ -1211,6 +1211,14 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         d_sh = torch.from_numpy(shadow.view(np.float32).reshape(-1, 8).copy()).to(dev)
         d_prev = torch.from_numpy(prev.view(np.int32).copy()).to(dev)
         d_occ = torch.empty(len(shadow), dtype=torch.int32, device=dev)
+        if not args.no_tune:
+            # the pass's trace launch takes the context's shape: tune it on
+            # the same any-hit rays
+            tuned, _ = ctx.autotune([(scene, d_sh, d_prev, d_occ, 1)], reps=5, force=True, plain=True)
+            ctx.set_launch_params(**tuned)
+            layout = tuned["layout"]
+            cfg = dict(cfg, layout=LAYOUT_NAMES[layout], launch=ctx.launch_params,
+                       launch_chosen_by="igxrt_autotune with IGXRT_TUNE_PLAIN on the pass's any-hit rays")
         fused = lambda: ctx.trace_shadow_mask(scene, d_pix, d_obj, w, h, 1, out=d_mask)
         plain = lambda: ctx.trace_any(scene, d_sh, d_prev, out=d_occ)
         for _ in range(args.warmup):
@@ -1280,9 +1288,14 @@ def run_mixed_bench(args, rank: int, world: int, local_rank: int):
     bvh = BVH.build_mixed(sc["tris"], sc["spheres"], sc["cubes"], sc["planes"])
     build_s = time.perf_counter() - t0
     scene = ctx.create_scene(bvh=bvh)
-    layout = ctx.launch_params["layout"]
     d_rays = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
     out = torch.empty((len(rays), 4), dtype=torch.float32, device=dev)
+    tuned_by = "default launch shape"
+    if not args.no_tune:
+        tuned, _ = ctx.autotune([(scene, d_rays, None, out, 0)], reps=5, force=True, plain=True)
+        ctx.set_launch_params(**tuned)
+        tuned_by = "igxrt_autotune with IGXRT_TUNE_PLAIN on the rays"
+    layout = ctx.launch_params["layout"]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     fn = lambda: ctx.trace_closest(scene, d_rays, out=out)
     for _ in range(args.warmup):
@@ -1308,7 +1321,7 @@ def run_mixed_bench(args, rank: int, world: int, local_rank: int):
     cfg = {"workload": "mixed_1m_tris_64k_spheres_64k_cubes_4_planes_4m_incoherent",
            "triangles": len(sc["tris"]), "spheres": len(sc["spheres"]), "cubes": len(sc["cubes"]),
            "planes": planes, "rays_per_step": n, "layout": LAYOUT_NAMES[layout],
-           "launch": ctx.launch_params, "bvh_build_s": round(build_s, 2),
+           "launch": ctx.launch_params, "launch_chosen_by": tuned_by, "bvh_build_s": round(build_s, 2),
            "l2": "256 MiB buffer written between timed steps"}
     line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms, cfg,
                  roofline=_roofline(b, ms, f"trace_kernel<{LAYOUT_NAMES[layout]},closest,mixed>",

@@ -23,7 +23,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["bvh_build.cpp", "capi.cpp", "autotune.cpp", "server.cpp", "trace_kernels.cu",
            "batch.cu", "shadow.cu", "gbuffer.cu", "refit.cu", "lbvh.cu", "static_scratch.cu"]
-HEADERS = ["internal.h", "engine.h", "traverse.cuh", "geometry.cuh", "share.cuh"]
+HEADERS = ["internal.h", "engine.h", "traverse.cuh", "geometry.cuh", "share.cuh", "gbuffer.cuh"]
 
 
 def nvcc_path() -> str:

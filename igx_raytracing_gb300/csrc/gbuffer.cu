@@ -1,19 +1,14 @@
 // gbuffer.cu — the reference's primary pass (raygen.comp) as one kernel:
-// primary-ray generation, closest hit and the shader's two output encodings.
-//
-// Every step follows the shader's binary32 expression order with separately
-// rounded operations: the screen mapping of calculateScreen
-// (res/shaders/camera.glsl:72-87, 113-116), the hit encoding of
-// raygen.comp:39-51, decodeSpheremap / interpolate / encodeNormal
-// (res/shaders/primitive.glsl:85-104, 146-151) for the vertex normal of
-// trace.glsl:48-57 (for a sphere, cube or plane of a mixed scene, its
-// geometry normal, trace.glsl:59-63).  A warp covers an 8x4 pixel tile so
-// neighbouring primary rays traverse together.
-#include <cuda_fp16.h>
-
+// primary-ray generation, closest hit and the shader's two output encodings
+// (gbuffer.cuh has the pieces and their reference lines; for a sphere, cube
+// or plane hit of a mixed scene the object normal is its geometry normal,
+// trace.glsl:59-63).  A warp covers an 8x4 pixel tile: its pixels trace
+// together and are written together (four 128-byte row segments, which
+// cross NVLink-C2C as whole lines when the images are in host memory).
 #include <algorithm>
 
 #include "engine.h"
+#include "gbuffer.cuh"
 #include "traverse.cuh"
 
 namespace igxrt {
@@ -22,63 +17,16 @@ struct GbufferArgs {
     const float4* nodes;
     const float4* prims;
     uint32_t node_count;
-    const igxrt_triangle* tris;
     uint32_t tri_count;       // mixed scenes: objects below this id are triangles
     const float4* planes;     // mixed scenes: planes outside the tree
     uint32_t plane_count;
     uint32_t plane_base;
-    igxrt_camera cam;
-    float inv_w, inv_h;
-    uint32_t tiles_x, tiles;
-    float4* dir_object;
-    float4* uv_normal;
+    GbufferSink g;            // camera, triangles and the two images
+    uint32_t tiles;
     uint32_t* status;
     uint32_t sh_depth;
     uint32_t phase_break;  // node_phase's early end (igxrt_launch_params.phase_break)
 };
-
-__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
-    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
-}
-
-// decodeSpheremap, primitive.glsl:95-104.
-__device__ __forceinline__ float3 decode_spheremap(uint32_t n) {
-    const float x = __half2float(__ushort_as_half((unsigned short)(n & 0xffffu)));
-    const float y = __half2float(__ushort_as_half((unsigned short)(n >> 16)));
-    // l = dot(vec3(nn, 1), -vec3(nn, -1))
-    const float l = dot3(x, y, 1.0f, -x, -y, 1.0f);
-    const float s = __fsqrt_rn(l);
-    const float sx = __fmul_rn(x, s), sy = __fmul_rn(y, s);
-    // vec3(nn, l) * 2 + vec3(0, 0, -1)
-    return make_float3(__fadd_rn(__fmul_rn(sx, 2.0f), 0.0f), __fadd_rn(__fmul_rn(sy, 2.0f), 0.0f),
-                       __fadd_rn(__fmul_rn(l, 2.0f), -1.0f));
-}
-
-// encodeNormal, primitive.glsl:85-88.
-__device__ __forceinline__ uint2 encode_normal(float3 n) {
-    const float len = __fsqrt_rn(dot3(n.x, n.y, n.z, n.x, n.y, n.z));
-    const float qx = __fdiv_rn(n.x, len), qy = __fdiv_rn(n.y, len), qz = __fdiv_rn(n.z, len);
-    const uint32_t hx = __float2uint_rz(__fmul_rn(__fadd_rn(__fmul_rn(qx, 0.5f), 0.5f), 65535.0f));
-    const uint32_t hy = __float2uint_rz(__fmul_rn(__fadd_rn(__fmul_rn(qy, 0.5f), 0.5f), 65535.0f));
-    const uint32_t hz = __float2uint_rz(__fmul_rn(__fadd_rn(__fmul_rn(qz, 0.5f), 0.5f), 65535.0f));
-    return make_uint2((hx << 16) | hy, hz);
-}
-
-// calculatePrimary / calculateScreen (camera.glsl:72-87, 113-116): the unit
-// direction of pixel (x, y), every operation rounded separately.
-__device__ __forceinline__ float3 camera_dir(const igxrt_camera& c, float inv_w, float inv_h, uint32_t x,
-                                             uint32_t y) {
-    const float cx = __fmul_rn(__fadd_rn((float)x, c.jitter_x), inv_w);
-    const float cy = __fsub_rn(1.0f, __fmul_rn(__fadd_rn((float)y, c.jitter_y), inv_h));
-    float d[3];
-    for (int k = 0; k < 3; ++k) {
-        const float right = __fsub_rn(c.p1[k], c.p0[k]), up = __fsub_rn(c.p2[k], c.p0[k]);
-        const float pos = __fadd_rn(__fadd_rn(c.p0[k], __fmul_rn(cx, right)), __fmul_rn(cy, up));
-        d[k] = __fsub_rn(pos, c.eye[k]);
-    }
-    const float len = __fsqrt_rn(dot3(d[0], d[1], d[2], d[0], d[1], d[2]));
-    return make_float3(__fdiv_rn(d[0], len), __fdiv_rn(d[1], len), __fdiv_rn(d[2], len));
-}
 
 // The primary rays of igxrt_trace_gbuffer as records: {eye, 0, dir, noHit}.
 __global__ void camera_rays_kernel(igxrt_camera c, float inv_w, float inv_h, float4* rays) {
@@ -142,32 +90,15 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
     st.sp = 0;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const igxrt_camera& c = a.cam;
+    const GbufferSink& g = a.g;
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < a.tiles; w += warps) {
-        const uint32_t ty = w / a.tiles_x, tx = w - ty * a.tiles_x;
-        const uint32_t x = tx * 8u + (lane & 7u), y = ty * 4u + (lane >> 3);
-        // the tile's pixels inside the image trace together (trace_warp);
-        // the lanes outside it take part in the warp's ballots only
-        const bool inside = x < c.width && y < c.height;
-        const float3 dir = camera_dir(c, a.inv_w, a.inv_h, inside ? x : 0u, inside ? y : 0u);
-        const float dx = dir.x, dy = dir.y, dz = dir.z;
-        RayState r;
-        r.ox = c.eye[0];
-        r.oy = c.eye[1];
-        r.oz = c.eye[2];
-        r.dx = dx;
-        r.dy = dy;
-        r.dz = dz;
-        r.ix = __frcp_rn(safe_dir(dx));
-        r.iy = __frcp_rn(safe_dir(dy));
-        r.iz = __frcp_rn(safe_dir(dz));
-        r.oix = __fmul_rn(r.ox, r.ix);
-        r.oiy = __fmul_rn(r.oy, r.iy);
-        r.oiz = __fmul_rn(r.oz, r.iz);
-        r.tmin = 0.f;
-        r.tmin_box = 0.f;
-        r.tmax_eff = IGXRT_NO_HIT;
-        r.prev = IGXRT_NO_RAY_HIT;
+        // tile w's pixel of this lane (gbuffer_pixel's order, 32 indices per tile);
+        // the tile's pixels inside the image trace together (trace_warp), the
+        // lanes outside it take part in the warp's ballots only
+        uint32_t x, y;
+        const bool inside = gbuffer_pixel(g, w * 32u + lane, x, y);
+        const RayState r = camera_ray_state(g.cam, camera_dir(g.cam, g.inv_w, g.inv_h, inside ? x : 0u,
+                                                              inside ? y : 0u));
         BestHit best;
         bool overflow = false;
         uint32_t rec = 0;
@@ -180,32 +111,59 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
             atomicOr(a.status, gave_up);
         if (!inside)
             continue;
-        const size_t px = (size_t)y * c.width + x;
+        const size_t px = (size_t)y * g.cam.width + x;
         // raygen.comp:39-44: a miss is hitT == noHit
-        if (best.t < IGXRT_NO_HIT) {
-            const uint32_t object = MIXED ? id_of_prio(best.prim) : best.prim;
-            a.dir_object[px] = make_float4(__fmul_rn(dx, best.t), __fmul_rn(dy, best.t),
-                                           __fmul_rn(dz, best.t), __uint_as_float(object));
-            if (MIXED && object >= a.tri_count) {
-                const uint2 e = encode_normal(mixed_geometry_normal(r, a.prims, a.planes, rec, best.t));
-                a.uv_normal[px] = make_float4(best.u, best.v, __uint_as_float(e.x), __uint_as_float(e.y));
-                continue;
-            }
-            const igxrt_triangle& t = a.tris[object];
-            const float3 n0 = decode_spheremap(t.n0), n1 = decode_spheremap(t.n1),
-                         n2 = decode_spheremap(t.n2);
-            // interpolate(n0, n1, n2, uv): (u*n1 + v*n2) + (1 - u - v)*n0
-            const float u = best.u, v = best.v, bw = __fsub_rn(__fsub_rn(1.0f, u), v);
-            const float3 n = make_float3(
-                __fadd_rn(__fadd_rn(__fmul_rn(u, n1.x), __fmul_rn(v, n2.x)), __fmul_rn(bw, n0.x)),
-                __fadd_rn(__fadd_rn(__fmul_rn(u, n1.y), __fmul_rn(v, n2.y)), __fmul_rn(bw, n0.y)),
-                __fadd_rn(__fadd_rn(__fmul_rn(u, n1.z), __fmul_rn(v, n2.z)), __fmul_rn(bw, n0.z)));
-            const uint2 e = encode_normal(n);
-            a.uv_normal[px] = make_float4(u, v, __uint_as_float(e.x), __uint_as_float(e.y));
-        } else {
-            a.dir_object[px] = make_float4(dx, dy, dz, __uint_as_float(IGXRT_NO_RAY_HIT));
+        const bool hit = best.t < IGXRT_NO_HIT;
+        if (MIXED && hit && id_of_prio(best.prim) >= a.tri_count) {
+            const uint32_t object = id_of_prio(best.prim);
+            g.dir_object[px] = make_float4(__fmul_rn(r.dx, best.t), __fmul_rn(r.dy, best.t),
+                                           __fmul_rn(r.dz, best.t), __uint_as_float(object));
+            const uint2 e = encode_normal(mixed_geometry_normal(r, a.prims, a.planes, rec, best.t));
+            g.uv_normal[px] = make_float4(best.u, best.v, __uint_as_float(e.x), __uint_as_float(e.y));
+            continue;
         }
+        BestHit tri = best;
+        if (MIXED)
+            tri.prim = id_of_prio(best.prim);
+        write_gbuffer_triangle(g, px, r.dx, r.dy, r.dz, tri, hit);
     }
+}
+
+// The tile kernel: a warp per 8x4 tile, a grid of at most the resident
+// CTAs striding over the tiles.
+igxrt_status launch_tiles(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_launch_params& p,
+                          GbufferArgs& a, cudaStream_t stream) {
+    a.nodes = reinterpret_cast<const float4*>(scene->nodes[p.layout]);
+    a.prims = reinterpret_cast<const float4*>(scene->prims);
+    a.node_count = scene->node_count[p.layout];
+    a.tri_count = scene->info.triangle_count;
+    a.planes = reinterpret_cast<const float4*>(scene->planes);
+    a.plane_count = scene->plane_count;
+    a.plane_base = scene->plane_base;
+    a.status = status_word(ctx);
+    a.sh_depth = p.stack_depth;
+    a.phase_break = p.phase_break;
+    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
+    auto fn = scene->mixed ? (p.layout == B8 ? gbuffer_kernel<B8, true>
+                              : p.layout == B4 ? gbuffer_kernel<B4, true> : gbuffer_kernel<B2, true>)
+                           : (p.layout == B8 ? gbuffer_kernel<B8, false>
+                              : p.layout == B4 ? gbuffer_kernel<B4, false> : gbuffer_kernel<B2, false>);
+    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
+    int per_sm = 0;
+    cudaError_t e = allow_smem((const void*)fn, smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
+    if (e != cudaSuccess || per_sm < 1)
+        return e != cudaSuccess ? cuda_fail(ctx, e, "occupancy query")
+                                : fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "no resident CTA");
+    const uint64_t wpb = p.block_size / 32;
+    const uint32_t grid = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, (a.tiles + wpb - 1) / wpb));
+    fn<<<grid, p.block_size, smem, stream>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "g-buffer kernel launch");
+    return IGXRT_OK;
 }
 
 }  // namespace igxrt
@@ -264,44 +222,17 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
                     "a buffer is not device memory: pass IGXRT_TRACE_HOST_MEMORY for host arrays");
     }
     GbufferArgs a;
-    a.nodes = reinterpret_cast<const float4*>(scene->nodes[p.layout]);
-    a.prims = reinterpret_cast<const float4*>(scene->prims);
-    a.node_count = scene->node_count[p.layout];
-    a.tris = scene->tris;
-    a.tri_count = scene->info.triangle_count;
-    a.planes = reinterpret_cast<const float4*>(scene->planes);
-    a.plane_count = scene->plane_count;
-    a.plane_base = scene->plane_base;
-    a.cam = *cam;
-    a.inv_w = 1.0f / (float)cam->width;
-    a.inv_h = 1.0f / (float)cam->height;
-    a.tiles_x = (cam->width + 7) / 8;
-    a.tiles = a.tiles_x * ((cam->height + 3) / 4);
-    a.dir_object = d_do;
-    a.uv_normal = d_uv;
-    a.status = status_word(ctx);
-    a.sh_depth = p.stack_depth;
-    a.phase_break = p.phase_break;
-    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
-    auto fn = scene->mixed ? (p.layout == B8 ? gbuffer_kernel<B8, true>
-                              : p.layout == B4 ? gbuffer_kernel<B4, true> : gbuffer_kernel<B2, true>)
-                           : (p.layout == B8 ? gbuffer_kernel<B8, false>
-                              : p.layout == B4 ? gbuffer_kernel<B4, false> : gbuffer_kernel<B2, false>);
-    const size_t smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
-    int per_sm = 0;
-    cudaError_t e = allow_smem((const void*)fn, smem);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, (int)p.block_size, smem);
-    if (e != cudaSuccess || per_sm < 1)
-        return e != cudaSuccess ? cuda_fail(ctx, e, "occupancy query")
-                                : fail(ctx, IGXRT_ERROR_INVALID_ARGUMENT, "no resident CTA");
-    const uint64_t wpb = p.block_size / 32;
-    const uint32_t grid = (uint32_t)std::max<uint64_t>(
-        1, std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, (a.tiles + wpb - 1) / wpb));
-    fn<<<grid, p.block_size, smem, stream>>>(a);
-    e = cudaGetLastError();
-    if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "g-buffer kernel launch");
+    a.g.tris = scene->tris;
+    a.g.cam = *cam;
+    a.g.inv_w = 1.0f / (float)cam->width;
+    a.g.inv_h = 1.0f / (float)cam->height;
+    a.g.tiles_x = (cam->width + 7) / 8;
+    a.g.dir_object = d_do;
+    a.g.uv_normal = d_uv;
+    a.tiles = a.g.tiles_x * ((cam->height + 3) / 4);
+    if ((st = launch_tiles(ctx, scene, p, a, stream)) != IGXRT_OK)
+        return st;
+    cudaError_t e = cudaSuccess;
     if (!host)
         return IGXRT_OK;
     if (staged) {
@@ -315,6 +246,8 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
         return cuda_fail(ctx, e, "g-buffer pass");
     return read_status(ctx);
 }
+
+
 
 extern "C" igxrt_status igxrt_camera_rays(igxrt_context* ctx, const igxrt_camera* cam, igxrt_ray* rays,
                                           uint32_t flags, void* stream_ptr) {

@@ -52,10 +52,13 @@ def test_oracle_gbuffer_encodes_hits_and_misses():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("route", ["host", "device"])
 @pytest.mark.parametrize("layout", [0, 1, 2])
 @pytest.mark.parametrize("dims,jitter", [((61, 37), (0.5, 0.5)), ((8, 4), (0.0, 0.0)),
                                          ((130, 67), (0.123, 0.877))])
-def test_gbuffer_matches_oracle(ctx, layout, dims, jitter):
+def test_gbuffer_matches_oracle(ctx, layout, dims, jitter, route):
+    """Host images (written in place) and device images, on images whose
+    last tile row and column lie partly outside."""
     w, h = dims
     tris = normals_scene()
     cam = scenes.camera_record(w, h, eye=(0.5, -1.2, 0.6), target=(0.5, 0.5, 0.45), jitter=jitter)
@@ -65,7 +68,16 @@ def test_gbuffer_matches_oracle(ctx, layout, dims, jitter):
     ctx.set_launch_params(layout=layout)
     scene = ctx.create_scene(tris)
     uv = np.full((h, w, 4), -3.0, dtype=np.float32)
-    g_do, g_uv = ctx.trace_gbuffer(scene, cam, uv_normal=uv)
+    if route == "device":
+        import torch
+
+        d_do = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+        d_uv = torch.from_numpy(uv).cuda()
+        ctx.trace_gbuffer(scene, cam, d_do, d_uv)
+        torch.cuda.synchronize()
+        g_do, g_uv = d_do.cpu().numpy(), d_uv.cpu().numpy()
+    else:
+        g_do, g_uv = ctx.trace_gbuffer(scene, cam, uv_normal=uv)
     ctx.set_launch_params(**saved)
     assert np.array_equal(bits(g_do), bits(e_do))
     assert np.array_equal(bits(g_uv), bits(e_uv))

@@ -88,6 +88,55 @@ def test_sphere_step_full_size(ctx, sphere):
     scene.close()
 
 
+def test_gbuffer_1080p_full_size(ctx, sphere):
+    """The raygen pass at 1920x1080 over the 1M-triangle sphere, into device
+    images and into pinned host images written in place.  Expected images from
+    the oracle: its camera rays, its CPU traversal of the engine's tree
+    (checked on every pixel above against its own tree and brute force),
+    dir * t and the object id on every pixel, and on a seeded sample of 65,536
+    hit pixels the barycentrics and encodeNormal of the interpolated vertex
+    normal (raygen.comp:39-51); misses leave uv_normal as it was."""
+    import torch
+
+    tris, _, bvh, otree = sphere
+    w, h = 1920, 1080
+    cam = scenes.camera_record(w, h, eye=(0.0, -3.0, 0.0), target=(0.0, 0.0, 0.0))
+    rays = pyoracle.camera_rays(cam)
+    nodes, prims = bvh.arrays(0)
+    e = pyoracle.bvh_trace(0, nodes, prims, rays)
+    hit = e["prim"] != 0xFFFFFFFF
+    assert hit.any() and (~hit).any()
+    d = rays["dir"].astype(np.float32)
+    exp_do = np.zeros((w * h, 4), np.float32)
+    exp_do[:, :3] = np.where(hit[:, None], d * e["t"][:, None].astype(np.float32), d)
+    exp_do[:, 3] = e["prim"].view(np.float32)
+    sample = _subset(int(hit.sum()), 65536, 7)
+    px = np.nonzero(hit)[0][sample]
+    t = tris[e["prim"][px]]
+    n0, n1, n2 = (pyoracle.decode_spheremap(t[f]) for f in ("n0", "n1", "n2"))
+    u = e["u"][px][:, None].astype(np.float32)
+    v = e["v"][px][:, None].astype(np.float32)
+    n = (u * n1 + v * n2) + ((np.float32(1) - u) - v) * n0
+    enc = pyoracle.encode_normal(n)
+    exp_uv = np.concatenate([u, v, enc.view(np.float32)], axis=1)
+    scene = ctx.create_scene(bvh=bvh)
+    fill = np.float32(-5.0)
+    d_do = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+    d_uv = torch.full((h, w, 4), float(fill), dtype=torch.float32, device="cuda")
+    ctx.trace_gbuffer(scene, cam, d_do, d_uv)
+    torch.cuda.synchronize()
+    h_do = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory().numpy()
+    h_uv = torch.full((h, w, 4), float(fill), dtype=torch.float32).pin_memory().numpy()
+    ctx.trace_gbuffer(scene, cam, h_do, h_uv)
+    for what, g_do, g_uv in (("device", d_do.cpu().numpy(), d_uv.cpu().numpy()), ("host", h_do, h_uv)):
+        g_do = g_do.reshape(-1, 4)
+        g_uv = g_uv.reshape(-1, 4)
+        bad = np.nonzero((g_do.view(np.uint32) != exp_do.view(np.uint32)).any(axis=1))[0]
+        assert len(bad) == 0, f"{what}: dir_object differs on {len(bad)} pixels, first {bad[:8]}"
+        assert np.array_equal(g_uv[px].view(np.uint32), exp_uv.view(np.uint32)), f"{what}: uv_normal differs"
+        assert (g_uv[~hit] == fill).all(), f"{what}: a miss wrote uv_normal"
+
+
 @pytest.mark.parametrize("ntris,variant", [(1_048_576, 1), (2_097_152, 0)])
 def test_incoherent_full_size(ctx, ntris, variant):
     """Config 3 (2M triangles) and its 1M variant: 4,194,304 incoherent rays."""

@@ -93,6 +93,13 @@ igxrt_status allocate_scene(igxrt_context* ctx, const igxrt_bvh_info& info, uint
 void node_parents(const igxrt_bvh& bvh, std::vector<uint32_t>& parents2,
                   std::vector<uint32_t>& parents4);
 
+// Camera rays as a traversal launch's ray source: ray i is the primary ray
+// of pixel (i mod width, i / width) (igxrt_trace_gbuffer's first step).
+struct CameraSource {
+    igxrt_camera cam;
+    float inv_w, inv_h;
+};
+
 // One traversal launch over `count` rays of one scene (device pointers).
 struct TraceRequest {
     const igxrt_scene* scene;
@@ -110,6 +117,9 @@ struct TraceRequest {
     // IGXRT_TRACE_INDEPENDENT: the kernel need not wait for the kernel
     // queued before it on the stream
     bool independent = false;
+    // non-null: the rays are this camera's, one per pixel (closest hit on a
+    // triangle scene; `rays` and `prev` unused)
+    const CameraSource* camera = nullptr;
 };
 
 // Records `msg` as the context's last error and returns `st`.

@@ -1,10 +1,17 @@
-// gbuffer.cu — the reference's primary pass (raygen.comp) as one kernel:
-// primary-ray generation, closest hit and the shader's two output encodings
-// (gbuffer.cuh has the pieces and their reference lines; for a sphere, cube
-// or plane hit of a mixed scene the object normal is its geometry normal,
-// trace.glsl:59-63).  A warp covers an 8x4 pixel tile: its pixels trace
-// together and are written together (four 128-byte row segments, which
-// cross NVLink-C2C as whole lines when the images are in host memory).
+// gbuffer.cu — the reference's primary pass (raygen.comp): primary-ray
+// generation, closest hit and the shader's two output encodings (gbuffer.cuh
+// has the pieces and their reference lines).
+//
+// Two forms, the same images bit for bit.  Triangle scenes whose images are
+// in device memory (or staged through it) trace the camera's rays with the
+// persistent trace kernel (trace_kernels.cu, rays made in the kernel), which
+// leaves each pixel's hit record in dir_object; an encoding kernel then turns
+// the records into the two images, one thread per pixel.  Mixed scenes (a
+// sphere, cube or plane hit's object normal is its geometry normal,
+// trace.glsl:59-63) and host images written in place use the tile kernel:
+// a warp per 8x4 tile, its pixels traced together and written together (four
+// 128-byte row segments, which cross NVLink-C2C as whole lines where single
+// pixels finishing one at a time would not).
 #include <algorithm>
 
 #include "engine.h"
@@ -129,6 +136,24 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufferArgs a) {
     }
 }
 
+// After the camera-ray trace: pixel i's hit record {t, u, v, prim} (the
+// trace kernel's output, written into dir_object) becomes its two images.
+// The direction is the camera's again (camera_dir, the trace's own rays).
+__global__ void __launch_bounds__(256) gbuffer_encode_kernel(GbufferSink g, uint32_t pixels) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pixels)
+        return;
+    const float4 h = g.dir_object[i];
+    const uint32_t y = i / g.cam.width, x = i - y * g.cam.width;
+    const float3 d = camera_dir(g.cam, g.inv_w, g.inv_h, x, y);
+    BestHit best;
+    best.t = h.x;
+    best.u = h.y;
+    best.v = h.z;
+    best.prim = __float_as_uint(h.w);
+    write_gbuffer_triangle(g, i, d.x, d.y, d.z, best, best.prim != IGXRT_NO_RAY_HIT);
+}
+
 // The tile kernel: a warp per 8x4 tile, a grid of at most the resident
 // CTAs striding over the tiles.
 igxrt_status launch_tiles(igxrt_context* ctx, const igxrt_scene* scene, const igxrt_launch_params& p,
@@ -230,9 +255,20 @@ extern "C" igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scen
     a.g.dir_object = d_do;
     a.g.uv_normal = d_uv;
     a.tiles = a.g.tiles_x * ((cam->height + 3) / 4);
-    if ((st = launch_tiles(ctx, scene, p, a, stream)) != IGXRT_OK)
-        return st;
     cudaError_t e = cudaSuccess;
+    if (!scene->mixed && (!host || staged)) {
+        CameraSource cs{*cam, a.g.inv_w, a.g.inv_h};
+        TraceRequest req{scene, nullptr, nullptr, (uint32_t)pixels, 0, reinterpret_cast<igxrt_hit*>(d_do),
+                         nullptr, nullptr, nullptr};
+        req.camera = &cs;
+        if ((st = launch_trace(ctx, req, p, stream)) != IGXRT_OK)
+            return st;
+        gbuffer_encode_kernel<<<(uint32_t)((pixels + 255) / 256), 256, 0, stream>>>(a.g, (uint32_t)pixels);
+        if ((e = cudaGetLastError()) != cudaSuccess)
+            return cuda_fail(ctx, e, "g-buffer encoding launch");
+    } else if ((st = launch_tiles(ctx, scene, p, a, stream)) != IGXRT_OK) {
+        return st;
+    }
     if (!host)
         return IGXRT_OK;
     if (staged) {

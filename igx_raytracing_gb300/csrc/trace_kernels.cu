@@ -10,6 +10,7 @@
 #include <algorithm>
 
 #include "engine.h"
+#include "gbuffer.cuh"
 #include "share.cuh"
 #include "traverse.cuh"
 
@@ -47,6 +48,7 @@ struct KernelArgs {
     // it and the queue word, so the slot needs no reset before its next launch
     uint32_t* exit_count;
     uint32_t independent;  // IGXRT_TRACE_INDEPENDENT: no wait for the kernel before
+    CameraSource camera;   // CAMERA kernels: the rays' camera
 };
 
 template <bool ANY, bool COUNT, bool MIXED>
@@ -89,9 +91,12 @@ constexpr int trace_kernel_regs(int layout, bool any, bool mixed) {
 // (oracle/trace_oracle.c); after that share_tail splits rays across lanes,
 // which visits the same subtrees in another order with the same result.
 // MIXED: scenes with spheres, cubes and planes (typed leaves, planes tested
-// when a ray starts, priority-coded best hit).
-template <int LAYOUT, bool ANY, bool COUNT, bool MIXED>
+// when a ray starts, priority-coded best hit).  CAMERA: ray i is made in the
+// kernel, the camera's primary ray of pixel i in row-major order
+// (igxrt_trace_gbuffer; closest hit on triangles).
+template <int LAYOUT, bool ANY, bool COUNT, bool MIXED, bool CAMERA = false>
 __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(KernelArgs a) {
+    static_assert(!CAMERA || (!ANY && !COUNT && !MIXED), "camera rays: closest hit on triangles");
     // Launched with programmatic stream serialization: unless the caller
     // stated independence, wait until the kernel queued before this one has
     // finished and its writes are visible (a no-op after any other work)
@@ -150,7 +155,13 @@ __global__ void __maxnreg__(trace_kernel_regs(LAYOUT, ANY, MIXED)) trace_kernel(
                 const uint32_t take = min(nidle - given, pk_end - pk_base);
                 if (!alive && rank >= given && rank < given + take) {
                     ray = pk_base + (rank - given);
-                    r = load_ray(a.rays, ray, a.prev ? __ldg(a.prev + ray) : IGXRT_NO_RAY_HIT);
+                    if (CAMERA) {
+                        const uint32_t y = ray / a.camera.cam.width, x = ray - y * a.camera.cam.width;
+                        r = camera_ray_state(a.camera.cam,
+                                             camera_dir(a.camera.cam, a.camera.inv_w, a.camera.inv_h, x, y));
+                    } else {
+                        r = load_ray(a.rays, ray, a.prev ? __ldg(a.prev + ray) : IGXRT_NO_RAY_HIT);
+                    }
                     best.t = r.tmax_eff;
                     best.u = 0.f;
                     best.v = 0.f;
@@ -253,6 +264,13 @@ static KernelFn select_kernel(uint32_t layout, bool any, bool count, bool mixed)
     return any ? trace_kernel<B2, true, false, false> : trace_kernel<B2, false, false, false>;
 }
 
+static KernelFn select_camera_kernel(uint32_t layout) {
+    constexpr int B2 = IGXRT_LAYOUT_BVH2, B4 = IGXRT_LAYOUT_BVH4, B8 = IGXRT_LAYOUT_BVH8;
+    return layout == B8   ? trace_kernel<B8, false, false, false, true>
+           : layout == B4 ? trace_kernel<B4, false, false, false, true>
+                          : trace_kernel<B2, false, false, false, true>;
+}
+
 namespace {
 
 // The launch shape and arguments every traversal launch shares: the kernel
@@ -269,7 +287,10 @@ struct TraceLaunch {
 igxrt_status prepare_trace(igxrt_context* ctx, const TraceRequest& req, const igxrt_launch_params& p,
                            TraceLaunch& l) {
     const igxrt_scene* s = req.scene;
-    l.fn = select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr, s->mixed);
+    if (req.camera && (s->mixed || req.mode != 0 || req.node_fetches))
+        return fail(ctx, IGXRT_ERROR_UNSUPPORTED, "camera rays are traced for closest hits on triangles");
+    l.fn = req.camera ? select_camera_kernel(p.layout)
+                      : select_kernel(p.layout, req.mode == 1, req.node_fetches != nullptr, s->mixed);
     l.smem = (size_t)p.stack_depth * p.block_size * kStackEntryBytes;
     int per_sm = 0;
     cudaError_t e = allow_smem((const void*)l.fn, l.smem);
@@ -308,6 +329,8 @@ igxrt_status prepare_trace(igxrt_context* ctx, const TraceRequest& req, const ig
     a.status = nullptr;
     a.exit_count = nullptr;
     a.independent = 0u;
+    if (req.camera)
+        a.camera = *req.camera;
     return IGXRT_OK;
 }
 

@@ -633,8 +633,8 @@ typedef struct igxrt_camera {
 } igxrt_camera;
 
 /*
- * Fused primary pass: raygen.comp (res/shaders/raygen.comp:16-52) with the
- * default projection as one kernel.  For pixel (x, y), y = loc.y:
+ * Primary pass: raygen.comp (res/shaders/raygen.comp:16-52) with the default
+ * projection, no ray buffer in between.  For pixel (x, y), y = loc.y:
  *   c = ((x, y) + jitter) * (1/width, 1/height), c.y = 1 - c.y
  *   dir = normalize(p0 + c.x*(p1 - p0) + c.y*(p2 - p0) - eye)   (camera.glsl:72-87, 113-116)
  *   hit = traceGeometry((eye, dir), noRayHit)
@@ -642,7 +642,11 @@ typedef struct igxrt_camera {
  *   dir_object = {dir*t, bits(object)} on a hit, {dir, bits(noRayHit)} on a miss (:39-44);
  *   uv_normal  = {u, v, bits(encodeNormal(objectNormal))} on a hit, not written on a miss (:46-51),
  * with objectNormal = interpolate(decodeSpheremap(n0), decodeSpheremap(n1),
- * decodeSpheremap(n2), uv) of the hit triangle (trace.glsl:48-57).
+ * decodeSpheremap(n2), uv) of the hit triangle (trace.glsl:48-57).  Device
+ * images of a triangle scene are written in two kernels (the persistent
+ * trace with rays made in the kernel leaves each pixel's hit record in
+ * dir_object, then one encoding thread per pixel); mixed scenes and host
+ * images written in place use one kernel of 8x4 pixel tiles.
  */
 igxrt_status igxrt_trace_gbuffer(igxrt_context* ctx, const igxrt_scene* scene,
                                  const igxrt_camera* camera, float* dir_object, float* uv_normal,

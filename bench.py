@@ -1124,9 +1124,11 @@ def _roofline(achieved_bytes: int, ms: float, kernel: str, traffic=None) -> dict
 def run_pass_bench(args, rank: int, world: int, local_rank: int):
     """--workload gbuffer | shadowmask on the 1M-triangle sphere at 1080p.
 
-    gbuffer: igxrt_trace_gbuffer, the reference's raygen.comp as one kernel
-    (camera rays, closest hit, dirObject and uvNormal encodings); compared
-    with igxrt_camera_rays + igxrt_trace_closest (no encodings).
+    gbuffer: igxrt_trace_gbuffer, the reference's raygen.comp (camera rays
+    made in the trace kernel, closest hit, then the dirObject and uvNormal
+    encodings; the e2e figure writes host images in place with the tile
+    kernel); compared with igxrt_camera_rays + igxrt_trace_closest (no
+    encodings).
     shadowmask: igxrt_trace_shadow_mask, nv_all.shadow.comp's any-hit rays
     toward the point light packed into ballot words (one sample); compared
     with igxrt_trace_any on the same rays (one word per ray)."""
@@ -1169,9 +1171,10 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         clk = clocks.stop()
         split_ms = statistics.mean(_event_ms(torch, split, args.steps, flush, stream))
         nf, pf = ctx.count_fetches(scene, rays, None, mode=0, layout=layout)
-        # per pixel: dirObject written (16 B); on a hit also uvNormal (16 B) and
-        # the hit triangle's normals (48 B); no ray is read
-        b = int(16 * len(rays) + (16 + 48) * int(hit.sum()) + NODE_BYTES[layout] * int(nf.sum(dtype=np.int64))
+        # per pixel: the trace's hit record written and read back by the
+        # encoding kernel (16 + 16 B), dirObject written (16 B); on a hit also
+        # uvNormal (16 B) and the hit triangle's normals (48 B); no ray is read
+        b = int(48 * len(rays) + (16 + 48) * int(hit.sum()) + NODE_BYTES[layout] * int(nf.sum(dtype=np.int64))
                 + PRIM_BYTES * int(pf.sum(dtype=np.int64)))
         hdo = torch.empty((h, w, 4), dtype=torch.float32).pin_memory().numpy()
         huv = torch.zeros((h, w, 4), dtype=torch.float32).pin_memory().numpy()
@@ -1185,7 +1188,8 @@ def run_pass_bench(args, rank: int, world: int, local_rank: int):
         n = w * h
         line = _line(args, world, world * n / (ms / 1e3) / 1e6, ms,
                      dict(cfg, workload="gbuffer_sphere_1m_1080p", rays_per_step=n),
-                     roofline=_roofline(b, ms, f"gbuffer_kernel<{LAYOUT_NAMES[layout]}>",
+                     roofline=_roofline(b, ms, f"trace_kernel<{LAYOUT_NAMES[layout]},closest,camera> + "
+                                               "gbuffer_encode_kernel",
                                         traffic_from_profiles("gbuffer_sphere_1m_1080p", "gbuffer", layout)),
                      e2e={"value": round(world * n / (e2e_ms / 1e3) / 1e6, 3), "unit": UNIT,
                           "h2d_bytes_per_step": 64, "d2h_bytes_per_step": 32 * n,

@@ -153,3 +153,28 @@ def test_gbuffer_host_routes_match_oracle(ctx, memory):
     hit = g_do[..., 3].view(np.uint32) != 0xFFFFFFFF
     assert hit.any() and (~hit).any()
     assert rays.tobytes() == ctx.camera_rays(cam).tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("route", ["host", "device"])
+def test_gbuffer_empty_scene_misses_everywhere(ctx, route):
+    """A scene without primitives: every pixel a miss ({dir, noRayHit}), the
+    caller's uv_normal untouched, in both forms."""
+    w, h = 37, 21
+    cam = scenes.camera_record(w, h, eye=(0.5, -1.2, 0.6), target=(0.5, 0.5, 0.45))
+    e_do, e_uv, _ = pyoracle.gbuffer(np.zeros(0, dtype=normals_scene().dtype), cam, uv_fill=-3.0)
+    scene = ctx.create_scene(np.zeros(0, dtype=normals_scene().dtype))
+    uv = np.full((h, w, 4), -3.0, dtype=np.float32)
+    if route == "device":
+        import torch
+
+        d_do = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+        d_uv = torch.from_numpy(uv).cuda()
+        ctx.trace_gbuffer(scene, cam, d_do, d_uv)
+        torch.cuda.synchronize()
+        g_do, g_uv = d_do.cpu().numpy(), d_uv.cpu().numpy()
+    else:
+        g_do, g_uv = ctx.trace_gbuffer(scene, cam, uv_normal=uv)
+    assert (g_do[..., 3].view(np.uint32) == 0xFFFFFFFF).all()
+    assert np.array_equal(bits(g_do), bits(e_do))
+    assert (g_uv == -3.0).all() and np.array_equal(bits(g_uv), bits(e_uv))

@@ -988,8 +988,8 @@ def measure_serve(args, ctx, device: int, world: int, duration: float) -> dict:
         # (the server's threads, its arena and the host cores come up to speed)
         for t in srv.replay(reqs[:n_warm], arrivals[:n_warm]):
             srv.wait(t)
-        clocks = ClockSampler(device, interval_ms=250, tag="_serve")
-        if with_clocks:
+        clocks = ClockSampler(device, interval_ms=args.serve_clock_ms, tag="_serve")
+        if with_clocks and args.serve_clock_ms > 0:
             clocks.start()
         tickets = srv.replay(reqs, arrivals)
         lat = np.zeros(n_req)
@@ -998,7 +998,8 @@ def measure_serve(args, ctx, device: int, world: int, duration: float) -> dict:
             w = srv.wait(t)
             lat[k] = 1e3 * (w["completed"] - w["arrival"])
             first, last = min(first, w["arrival"]), max(last, w["completed"])
-        clk = clocks.stop() if with_clocks else None
+        clk = (clocks.stop() if args.serve_clock_ms > 0 else {"sm_mhz": None, "reasons": ["not sampled"]}) \
+            if with_clocks else None
         st = srv.stats()
         st["span_s"] = last - first
         times = srv.batch_times()
@@ -1503,6 +1504,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: requests per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--streams", type=int, default=2, help="serve: batches in flight")
+    ap.add_argument("--serve-clock-ms", type=int, default=250,
+                    help="serve: nvidia-smi sampling interval during the serving pass (0: none)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 

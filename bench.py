@@ -707,9 +707,9 @@ def run_engine(args, rank: int, world: int, local_rank: int):
     if args.layout is not None:
         ctx.set_launch_params(layout=args.layout)
     line = measure_plain(args, ctx, dev, args.workload, world)
-    # the benchmark spec's other targets under the same run: the 1M- and
-    # 2M-triangle incoherent workloads (the roofline target is on the 1M
-    # variant), the 64-scene batch against 64 plain launches, and a serving run
+    # the workload's other targets in the same run: the 1M- and 2M-triangle
+    # incoherent workloads (the roofline target is on the 1M variant), the
+    # 64-scene batch against 64 plain launches, and a serving run
     if args.workload == "sphere" and world == 1 and not args.no_extras:
         for sub in ("incoherent1m", "incoherent"):
             log(f"bench: {sub}")

@@ -71,7 +71,7 @@ def sphere():
 
 
 def test_sphere_step_full_size(ctx, sphere):
-    """Config 2: 1,048,576 triangles; 2,073,600 primaries, then one bounce
+    """The 1M-triangle sphere step: 1,048,576 triangles; 2,073,600 primaries, then one bounce
     and one shadow ray per primary hit (prev_hit = the hit)."""
     tris, prim, bvh, otree = sphere
     scene = ctx.create_scene(bvh=bvh)
@@ -139,7 +139,7 @@ def test_gbuffer_1080p_full_size(ctx, sphere):
 
 @pytest.mark.parametrize("ntris,variant", [(1_048_576, 1), (2_097_152, 0)])
 def test_incoherent_full_size(ctx, ntris, variant):
-    """Config 3 (2M triangles) and its 1M variant: 4,194,304 incoherent rays."""
+    """Random triangles, 2M and 1M of them: 4,194,304 incoherent rays."""
     tris, rays = scenes.workload_incoherent(ntris, 4_194_304, variant=variant)
     bvh = BVH.build(tris)
     otree = pyoracle.bvh_build(tris)
@@ -158,7 +158,7 @@ def test_incoherent_full_size(ctx, ntris, variant):
 
 
 def test_batch_64_scenes_full_size(ctx):
-    """Config 4: the 64-scene batch (1K-512K triangles, 4K-2M rays per item,
+    """The 64-scene batch (1K-512K triangles, 4K-2M rays per item,
     20.6M rays) as one graph-captured launch; every item against the oracle."""
     import torch
 
@@ -191,7 +191,7 @@ def test_batch_64_scenes_full_size(ctx):
 
 
 def test_serving_sample_full_size_scenes(ctx):
-    """Config 5's 32 resident scenes (10K-2M triangles): 160 requests of its
+    """The serving workload's 32 resident scenes (10K-2M triangles): 160 requests of its
     request distribution (1K-1M rays, closest or any hit), replayed at
     2,000 requests/s through the server; every request against the oracle."""
     from igx_raytracing_gb300 import Server

@@ -1510,7 +1510,7 @@ def main():
     args.warmup = max(3, args.warmup)
 
     if "WORLD_SIZE" not in os.environ and args.gpus > 1:
-        # start one rank per GPU (the launch the driver uses for N > 1)
+        # start one rank per GPU, as torchrun does for N > 1
         cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
                "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
                os.path.abspath(__file__)] + sys.argv[1:]

@@ -1,8 +1,8 @@
 /*
  * oracle.h — CPU restatement of igx_raytracing's ray-query path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
- * engine and the timed CPU baseline; the engine never links, loads or calls
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the CUDA engine is
+ * tested against, and the timed CPU baseline; the engine never links, loads or calls
  * it.  Only the test suite, the smoke check and the benchmark's CPU-baseline
  * leg use it.
  *

@@ -1,8 +1,8 @@
 /*
  * trace_oracle.c — CPU restatement of igx_raytracing's ray-query path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA engine and the timed
- * CPU baseline.  The engine never links or calls this file.
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA engine is tested against,
+ * and the timed CPU baseline.  The engine never links or calls this file.
  *
  * Arithmetic contract (the same one the CUDA kernels follow):
  *   - IEEE binary32, round to nearest, denormals kept (no flush to zero);

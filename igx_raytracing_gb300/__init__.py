@@ -8,6 +8,6 @@ from ._capi import (HIT_DTYPE, LAYOUT_BVH2, LAYOUT_BVH4, LAYOUT_BVH8, NO_HIT, NO
                     TRIANGLE_DTYPE, IgxrtError, lib)
 from .api import BVH, Batch, Context, Scene, Server, as_rays, as_triangles, make_rays
 
-__all__ = ["BVH", "Batch", "Context", "Scene", "IgxrtError", "as_rays", "as_triangles", "make_rays", "lib",
+__all__ = ["BVH", "Batch", "Context", "Scene", "Server", "IgxrtError", "as_rays", "as_triangles", "make_rays", "lib",
            "HIT_DTYPE", "RAY_DTYPE", "TRIANGLE_DTYPE", "NO_HIT", "NO_RAY_HIT", "LAYOUT_BVH2",
            "LAYOUT_BVH4", "LAYOUT_BVH8"]

@@ -97,8 +97,6 @@ def test_graph_batch_replays_identically(ctx):
 
 
 def test_batch_rejects_host_arrays(ctx, engine_lib):
-    import ctypes as C
-
     from igx_raytracing_gb300 import _capi
 
     tris, rays = scenes.workload_small()

@@ -4,12 +4,10 @@ closest hit and the shader's output encodings.
 CPU: the oracle's decodeSpheremap / encodeNormal / interpolate restatement
 against the reference's own code (golden `normals`).  GPU: the kernel's two
 images against the oracle's, bit for bit."""
-import math
-
 import numpy as np
 import pytest
 
-from conftest import NO_HIT, bits, load_golden
+from conftest import bits, load_golden
 from igx_raytracing_gb300 import scenes
 from oracle import pyoracle
 

@@ -16,7 +16,7 @@ import pytest
 
 from conftest import NO_HIT, bits, load_golden
 from igx_raytracing_gb300 import BVH, IgxrtError, scenes
-from igx_raytracing_gb300._capi import CUBE_DTYPE, RAY_DTYPE
+from igx_raytracing_gb300._capi import CUBE_DTYPE
 from oracle import pyoracle
 
 UV_ULPS = 2

@@ -15,8 +15,6 @@ Each GPU result is compared bit for bit (prim, t, u, v; occlusion words):
 Disagreements are re-intersected in binary64 and printed (conftest.f64_report).
 The sphere's bounce and shadow rays start at its primary hits once those
 have been checked against the oracle."""
-import math
-
 import numpy as np
 import pytest
 

@@ -1,8 +1,6 @@
 """The fused shadow pass (nv_all.shadow.comp as one kernel) against the
 oracle's restatement: brute-force traceOcclusion per pixel and sample,
 ballot-packed at indexToLight (light.glsl:221-229)."""
-import math
-
 import numpy as np
 import pytest
 

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from igx_raytracing_gb300 import BVH, scenes
-from igx_raytracing_gb300._capi import HIT_DTYPE, RAY_DTYPE
+from igx_raytracing_gb300._capi import HIT_DTYPE
 from oracle import pyoracle
 
 pytestmark = pytest.mark.gpu
